@@ -1,0 +1,193 @@
+/*
+ * igsolve.h -- C-ABI of libigsolve.so, the GB300 (sm_103a) implementation of
+ * ion_gym's 3-D finite-difference Laplace field solve.
+ *
+ * Every solver entry point takes arrays in C order (nx, ny, nz), z
+ * contiguous, is synchronous, and returns an int status (IG_OK or one of the
+ * codes below).  ig_solve3d, ig_solve3d_mg and ig_cascadic_relres accept
+ * host (pageable or pinned) or device pointers alike (the copies resolve the
+ * direction by unified addressing); the V-cycle and basis entry points read
+ * their masks on the host and need host arrays.  A failing call leaves a message for ig_last_error() (per
+ * calling thread).  Masks are uint8 (0 / 1); potentials float64; theta, when
+ * given, float32 (6, nx, ny, nz) in the order (-x, +x, -y, +y, -z, +z);
+ * theta == NULL is the reference's theta=None.  stencil: 0 = "ghost_linear",
+ * 1 = "sw".  The calling thread's current CUDA device runs the solve.
+ *
+ * The FP64 entry points return the reference's bits: the same sweep counts,
+ * the same final delta and the same potential, node for node.
+ *
+ * Functions ending in _dev take DEVICE pointers and a cudaStream_t (as
+ * void*, NULL = the legacy default stream); they enqueue on that stream and,
+ * when they return a max, synchronize it.
+ */
+#ifndef IGSOLVE_H
+#define IGSOLVE_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------- */
+enum {
+  IG_OK = 0,
+  IG_NOT_CONVERGED = 1, /* SOR sweep cap (solver3d.py:287-293)               */
+  IG_STAGNATED = 2,     /* V-cycle stagnation (multigrid3d.py:708-724)       */
+  IG_CYCLE_CAP = 3,     /* V-cycle max_cycles (multigrid3d.py:726-731)       */
+  IG_INTERRUPTED = 4,   /* stop requested (multigrid3d.py:255-260, 655, 669) */
+  IG_BAD_ARG = 5,       /* invalid shape, stencil or pointer                 */
+  IG_CUDA_ERROR = 6,    /* a CUDA call failed; see ig_last_error()           */
+  IG_NO_DEVICE = 7      /* no CUDA device is visible                         */
+};
+
+/* Message of the last failing call on this thread ("" if none). */
+const char *ig_last_error(void);
+/* ABI version of this header. */
+int ig_abi_version(void);
+/* Number of visible CUDA devices (0 without a GPU; never fails). */
+int ig_device_count(void);
+
+/* ---- cooperative stop (multigrid3d.py:42, 61-79) ----------------------
+ * Replaces the threading.Event _STOP: request_stop() / clear_stop() set and
+ * clear it; the V-cycle polls it twice per cycle and the basis loop between
+ * bases, exactly where the reference polls _STOP. */
+void ig_request_stop(void);
+void ig_clear_stop(void);
+int ig_stop_requested(void);
+
+/* ---- solvers (host arrays, synchronous) -------------------------------- */
+
+/* solver3d.solve3d (solver3d.py:250-293): red-black SOR until the max
+ * |update| of a sweep pair is < tol, at most max_sweeps pairs.
+ * omega: the SOR factor (the caller passes optimal_omega(shape) for None).
+ * phi0: NULL for a zero start.  Out: phi (n), sweep pairs, final delta.
+ * IG_NOT_CONVERGED at the cap, with the last pair's delta. */
+int ig_solve3d(const uint8_t *fixed, const double *val, const float *theta,
+               long nx, long ny, long nz, double tol, long max_sweeps,
+               double omega, const double *phi0, int stencil, double *phi_out,
+               long *sweeps_out, double *delta_out);
+
+/* multigrid3d.solve3d_mg (multigrid3d.py:175-230), cascadic multigrid:
+ * levels by _coarsen_mask while min(shape) > min_coarse and the next level
+ * keeps every axis >= 3 (at most max_levels), coarsest solved to tol,
+ * intermediates to tol * level_tol_factor from the prolongated guess, fine
+ * level to tol with theta.  level_omega[L] is the SOR factor of level L
+ * (0 = fine); n_level_omega must be at least the number of levels.
+ * Out: fine phi, fine sweep pairs, fine delta. */
+int ig_solve3d_mg(const uint8_t *fixed, const double *val, const float *theta,
+                  long nx, long ny, long nz, double tol, long max_sweeps,
+                  int stencil, int min_coarse, int max_levels,
+                  double level_tol_factor, const double *level_omega,
+                  int n_level_omega, double *phi_out, long *sweeps_out,
+                  double *delta_out);
+
+/* multigrid3d.solve3d_vmg (multigrid3d.py:602-731), V-cycle multigrid with
+ * the recursive error-equation solve of _solve_err (multigrid3d.py:553-599).
+ * bottom_omega: optimal_omega() of the bottom error level's shape (<= 0:
+ * computed here with libm).  Out: phi, fine sweep pairs, final cycle delta,
+ * cycles run, and the previous cycle's delta (for the stagnation message).
+ * IG_STAGNATED / IG_CYCLE_CAP / IG_INTERRUPTED as the reference raises;
+ * accept_stagnation != 0 returns IG_OK with the stalled iterate. */
+int ig_solve3d_vmg(const uint8_t *fixed, const double *val, const float *theta,
+                   long nx, long ny, long nz, double tol, int max_cycles,
+                   int nu1, int nu2, int stencil, const double *phi0,
+                   int accept_stagnation, double bottom_omega, double *phi_out,
+                   long *sweeps_out, double *delta_out, int *cycles_out,
+                   double *prev_delta_out);
+
+/* One basis of multigrid3d.solve_bases_mg (multigrid3d.py:265-269): the
+ * V-cycle on the metal union with val = v_basis on `mask` and 0 elsewhere,
+ * built on the device from the mask.  Same outputs and statuses as
+ * ig_solve3d_vmg. */
+int ig_solve_basis_vmg(const uint8_t *metal, const uint8_t *mask,
+                       double v_basis, const float *theta, long nx, long ny,
+                       long nz, double tol, int max_cycles, int nu1, int nu2,
+                       int stencil, double bottom_omega, double *phi_out,
+                       long *sweeps_out, double *delta_out, int *cycles_out,
+                       double *prev_delta_out);
+
+/* One basis of solver3d.solve_bases (solver3d.py:308-319): SOR on the metal
+ * union with val = v_basis on `mask`.  Same outputs as ig_solve3d. */
+int ig_solve_basis_sor(const uint8_t *metal, const uint8_t *mask,
+                       double v_basis, const float *theta, long nx, long ny,
+                       long nz, double tol, long max_sweeps, double omega,
+                       int stencil, double *phi_out, long *sweeps_out,
+                       double *delta_out);
+
+/* Cascadic multigrid with a residual stopping rule (no reference
+ * counterpart; the quadrupole benchmark's rule): the same level hierarchy as
+ * ig_solve3d_mg, each level relaxed with red-black SOR at level_omega[L],
+ * the relative residual max|r| / max|r(phi_D)| (r: multigrid3d._residual,
+ * phi_D: the Dirichlet values, zero elsewhere) checked every check_every
+ * pairs; the coarsest and fine levels stop below rel_tol, intermediates
+ * below rel_tol * level_tol_factor.  Out: fine phi, fine pairs, fine
+ * relative residual, total pairs on all levels, and (levels_out) the level
+ * count. */
+int ig_cascadic_relres(const uint8_t *fixed, const double *val, long nx,
+                       long ny, long nz, double rel_tol, long max_sweeps,
+                       int min_coarse, int max_levels, double level_tol_factor,
+                       const double *level_omega, int n_level_omega,
+                       int check_every, double *phi_out, long *sweeps_out,
+                       double *relres_out, long *total_pairs_out,
+                       int *levels_out);
+
+/* ---- single kernels on device arrays ----------------------------------- */
+
+/* solver3d._sweep (solver3d.py:131-198); theta NULL = all ones.  The max
+ * |update| goes to *dmax_out (host), after a stream synchronize. */
+int ig_sweep_dev(double *phi, const uint8_t *fixed, const float *theta,
+                 long nx, long ny, long nz, double omega, int colour,
+                 int stencil, double *dmax_out, void *stream);
+/* multigrid3d._residual (multigrid3d.py:305-354). */
+int ig_residual_dev(const double *phi, const uint8_t *fixed,
+                    const float *theta, long nx, long ny, long nz, int stencil,
+                    double *out, void *stream);
+/* multigrid3d._sweep_rhs (multigrid3d.py:357-391). */
+int ig_sweep_rhs_dev(double *e, const uint8_t *fixed, const double *f,
+                     long nx, long ny, long nz, double omega, int colour,
+                     double *dmax_out, void *stream);
+/* multigrid3d._residual_rhs (multigrid3d.py:394-417). */
+int ig_residual_rhs_dev(const double *e, const uint8_t *fixed, const double *f,
+                        long nx, long ny, long nz, double *out, void *stream);
+/* multigrid3d._restrict_fw_njit (multigrid3d.py:420-455): out has the
+ * ((n+1)/2) coarse shape. */
+int ig_restrict_fw_dev(const double *fine, long nx, long ny, long nz,
+                       double *out, void *stream);
+/* multigrid3d._prolong_add_njit (multigrid3d.py:458-499). */
+int ig_prolong_add_dev(const double *coarse, long cx, long cy, long cz,
+                       double *out, const uint8_t *fixed, long nx, long ny,
+                       long nz, void *stream);
+/* multigrid3d._prolongate (multigrid3d.py:138-171). */
+int ig_prolongate_dev(const double *coarse, long cx, long cy, long cz,
+                      double *out, long nx, long ny, long nz, void *stream);
+/* multigrid3d._coarsen_fixed_any (multigrid3d.py:507-526). */
+int ig_coarsen_fixed_any_dev(const uint8_t *fixed, long nx, long ny, long nz,
+                             uint8_t *out, void *stream);
+/* multigrid3d._coarsen_mask (multigrid3d.py:85-135). */
+int ig_coarsen_mask_dev(const uint8_t *fixed, const double *val, long nx,
+                        long ny, long nz, uint8_t *fc, double *vc,
+                        void *stream);
+/* solver3d._residual_kernel (solver3d.py:366-386); every axis >= 2. */
+int ig_residual_audit_dev(const double *u, const uint8_t *fixed,
+                          const float *theta, long nx, long ny, long nz,
+                          double *out, void *stream);
+/* solver3d._err_sweep (solver3d.py:389-417); every axis >= 2. */
+int ig_err_sweep_dev(double *e, const uint8_t *fixed, const float *theta,
+                     const double *rhs, long nx, long ny, long nz,
+                     double omega, int colour, double *dmax_out, void *stream);
+
+/* ---- profiling of the timed sweep launches ----------------------------
+ * When enabled, the SOR loops bracket each batch of sweep launches with CUDA
+ * events on their own stream and accumulate the time and the number of
+ * launches that did work. */
+void ig_prof_enable(int on);
+void ig_prof_reset(void);
+void ig_prof_read(double *sweep_ms, long *sweep_launches, long *sweep_nodes);
+/* Kernel launches this library has issued since it was loaded. */
+long ig_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* IGSOLVE_H */

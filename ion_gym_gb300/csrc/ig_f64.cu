@@ -1,0 +1,756 @@
+// ig_f64.cu -- exact FP64 kernels of the 3-D Laplace solve on sm_103a.
+//
+// Each kernel returns the bits the reference's compiled float64 kernels
+// return on the same input (ion_gym physics/solver3d.py and
+// physics/multigrid3d.py, cited per kernel).  FP64 is the scarce pipe on
+// GB300 (about 1/64 of the FP32 rate), so the kernels spend it only where the
+// reference does: masks, indices, maxima and absolute values run on the
+// integer pipe, and the theta == 1 stencil divides by 6 in two FP64 operations
+// (ig::div6) instead of a full division.
+//
+// Layout: C-order (nx, ny, nz), z contiguous; theta (6, nx, ny, nz) float32.
+// Sweeps map one thread to one (i, j, k-pair) cell so a warp reads 64
+// consecutive doubles of a row and every lane does useful FP64 work; the
+// flattened index is split with 32-bit multiplicative division.
+#include <atomic>
+
+#include "ig_common.cuh"
+#include "ig_internal.h"
+
+namespace ig {
+
+std::atomic<long> g_launches{0};
+long launch_total() { return g_launches.load(); }
+
+namespace {
+
+constexpr int kThreads = 256;
+
+inline void counted() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+__device__ __forceinline__ uint32_t fdiv(uint32_t n, const FastDiv& f) {
+  return (__umulhi(n, f.m) + n) >> f.s;
+}
+
+struct SweepGeom {
+  long nx, ny, nz;
+  FastDiv div_kk, div_ny;
+  uint32_t total;  // nx*ny*nkk
+};
+
+inline SweepGeom sweep_geom(Dims d) {
+  SweepGeom g;
+  g.nx = d.nx;
+  g.ny = d.ny;
+  g.nz = d.nz;
+  const long nkk = (d.nz + 1) / 2;
+  g.div_kk = FastDiv((uint32_t)nkk);
+  g.div_ny = FastDiv((uint32_t)d.ny);
+  g.total = (uint32_t)(d.nx * d.ny * nkk);
+  return g;
+}
+
+struct FlatGeom {
+  long nx, ny, nz;
+  FastDiv div_nz, div_ny;
+  uint32_t total;
+};
+
+inline FlatGeom flat_geom(Dims d) {
+  FlatGeom g;
+  g.nx = d.nx;
+  g.ny = d.ny;
+  g.nz = d.nz;
+  g.div_nz = FastDiv((uint32_t)d.nz);
+  g.div_ny = FastDiv((uint32_t)d.ny);
+  g.total = (uint32_t)d.n();
+  return g;
+}
+
+inline unsigned blocks_for(size_t n) {
+  return (unsigned)((n + kThreads - 1) / kThreads);
+}
+
+// Early-exit test of the exact SOR loop (PairCtl in ig_internal.h).  Uniform
+// over the block, so a returning block skips the block reduction as a whole.
+__device__ __forceinline__ bool pair_skip(PairCtl* ctl, int colour, int lp) {
+  volatile PairCtl* c = ctl;
+  if (c->done) return true;
+  if (lp >= c->limit) return true;
+  if (colour == 0) {
+    unsigned long long a = 0, b = 0;
+    bool have = false;
+    if (lp > 0) {
+      a = c->slot[2 * lp - 2];
+      b = c->slot[2 * lp - 1];
+      have = true;
+    } else if (c->has_prev) {
+      a = c->prev[0];
+      b = c->prev[1];
+      have = true;
+    }
+    if (have) {
+      const double d = bits_to_double(a > b ? a : b);
+      if (d < c->tol) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) c->done = 1;
+        return true;
+      }
+    }
+  }
+  return false;
+}
+
+struct Nb {
+  size_t xm, xp, ym, yp, zm, zp;
+};
+
+__device__ __forceinline__ Nb neighbours(long i, long j, long k, long nx,
+                                         long ny, long nz) {
+  const size_t sy = (size_t)nz, sx = (size_t)ny * nz;
+  const size_t row = (size_t)i * sx + (size_t)j * sy;
+  Nb n;
+  n.xm = (size_t)lo_nb(i, nx) * sx + (size_t)j * sy + k;
+  n.xp = (size_t)hi_nb(i, nx) * sx + (size_t)j * sy + k;
+  n.ym = (size_t)i * sx + (size_t)lo_nb(j, ny) * sy + k;
+  n.yp = (size_t)i * sx + (size_t)hi_nb(j, ny) * sy + k;
+  n.zm = row + lo_nb(k, nz);
+  n.zp = row + hi_nb(k, nz);
+  return n;
+}
+
+// num and den of the theta-weighted stencil exactly as the reference forms
+// them (solver3d.py:169-191, multigrid3d.py:329-353).
+template <int KIND>
+__device__ __forceinline__ void theta_num_den(const double v[6],
+                                              const float* __restrict__ th,
+                                              size_t N, size_t p, double& num,
+                                              double& den) {
+  const float t0 = th[p], t1 = th[N + p], t2 = th[2 * N + p];
+  const float t3 = th[3 * N + p], t4 = th[4 * N + p], t5 = th[5 * N + p];
+  if (KIND == kThetaGhost) {
+    const double w0 = __drcp_rn((double)t0), w1 = __drcp_rn((double)t1);
+    const double w2 = __drcp_rn((double)t2), w3 = __drcp_rn((double)t3);
+    const double w4 = __drcp_rn((double)t4), w5 = __drcp_rn((double)t5);
+    num = __dmul_rn(v[0], w0);
+    num = __dadd_rn(num, __dmul_rn(v[1], w1));
+    num = __dadd_rn(num, __dmul_rn(v[2], w2));
+    num = __dadd_rn(num, __dmul_rn(v[3], w3));
+    num = __dadd_rn(num, __dmul_rn(v[4], w4));
+    num = __dadd_rn(num, __dmul_rn(v[5], w5));
+    den = __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(w0, w1), w2), w3), w4), w5);
+  } else {
+    const float sx = __fadd_rn(t0, t1), sy = __fadd_rn(t2, t3), sz = __fadd_rn(t4, t5);
+    const float a0 = __fmul_rn(t0, sx), a1 = __fmul_rn(t1, sx);
+    const float a2 = __fmul_rn(t2, sy), a3 = __fmul_rn(t3, sy);
+    const float a4 = __fmul_rn(t4, sz), a5 = __fmul_rn(t5, sz);
+    num = __ddiv_rn(v[0], (double)a0);
+    num = __dadd_rn(num, __ddiv_rn(v[1], (double)a1));
+    num = __dadd_rn(num, __ddiv_rn(v[2], (double)a2));
+    num = __dadd_rn(num, __ddiv_rn(v[3], (double)a3));
+    num = __dadd_rn(num, __ddiv_rn(v[4], (double)a4));
+    num = __dadd_rn(num, __ddiv_rn(v[5], (double)a5));
+    const double px = __drcp_rn((double)__fmul_rn(t0, t1));
+    const double py = __drcp_rn((double)__fmul_rn(t2, t3));
+    const double pz = __drcp_rn((double)__fmul_rn(t4, t5));
+    den = __dadd_rn(__dadd_rn(px, py), pz);
+  }
+}
+
+__device__ __forceinline__ double sum6(const double v[6]) {
+  return __dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(__dadd_rn(v[0], v[1]), v[2]), v[3]), v[4]), v[5]);
+}
+
+__device__ __forceinline__ void load6(const double* __restrict__ a, const Nb& n,
+                                      double v[6]) {
+  v[0] = a[n.xm];
+  v[1] = a[n.xp];
+  v[2] = a[n.ym];
+  v[3] = a[n.yp];
+  v[4] = a[n.zm];
+  v[5] = a[n.zp];
+}
+
+// solver3d._sweep (solver3d.py:131-198).
+template <int KIND, bool CTL>
+__global__ void __launch_bounds__(kThreads)
+k_sweep(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
+        const float* __restrict__ th, SweepGeom g, double omega, int colour,
+        unsigned long long* dslot, PairCtl* ctl, int lp) {
+  if (CTL) {
+    if (pair_skip(ctl, colour, lp)) return;
+    dslot = &ctl->slot[2 * lp + colour];
+  }
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  unsigned long long mb = 0;
+  if (t < g.total) {
+    const uint32_t ij = fdiv(t, g.div_kk);
+    const uint32_t kk = t - ij * g.div_kk.d;
+    const uint32_t i = fdiv(ij, g.div_ny);
+    const uint32_t j = ij - i * g.div_ny.d;
+    const long k = 2 * (long)kk + ((i + j + colour) & 1);
+    if (k < g.nz) {
+      const size_t p = ((size_t)i * g.ny + j) * g.nz + k;
+      if (!fixed[p]) {
+        const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
+        double v[6];
+        load6(phi, n, v);
+        const double old = phi[p];
+        double q;
+        if (KIND == kPlain) {
+          q = div6(sum6(v));
+        } else {
+          double num, den;
+          theta_num_den<KIND>(v, th, (size_t)g.nx * g.ny * g.nz, p, num, den);
+          q = __ddiv_rn(num, den);
+        }
+        const double nw = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(q, old)));
+        mb = absbits(__dsub_rn(nw, old));
+        phi[p] = nw;
+      }
+    }
+  }
+  block_max_to(mb, dslot);
+}
+
+// multigrid3d._residual (multigrid3d.py:305-354): num - den*phi, 0 at fixed.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads)
+k_residual(const double* __restrict__ phi, const uint8_t* __restrict__ fixed,
+           const float* __restrict__ th, FlatGeom g, double* __restrict__ out,
+           unsigned long long* absmax) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  unsigned long long mb = 0;
+  if (t < g.total) {
+    const uint32_t ij = fdiv(t, g.div_nz);
+    const uint32_t k = t - ij * g.div_nz.d;
+    const uint32_t i = fdiv(ij, g.div_ny);
+    const uint32_t j = ij - i * g.div_ny.d;
+    double r = 0.0;
+    if (!fixed[t]) {
+      const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
+      double v[6];
+      load6(phi, n, v);
+      if (KIND == kPlain) {
+        r = __dsub_rn(sum6(v), __dmul_rn(6.0, phi[t]));
+      } else if (KIND == kPlainSW) {
+        // unit legs: num = sum of v/2 (== sum/2 exactly), den = 3
+        r = __dsub_rn(__dmul_rn(sum6(v), 0.5), __dmul_rn(3.0, phi[t]));
+      } else {
+        double num, den;
+        theta_num_den<KIND>(v, th, g.total, t, num, den);
+        r = __dsub_rn(num, __dmul_rn(den, phi[t]));
+      }
+    }
+    if (out) out[t] = r;
+    mb = absbits(r);
+  }
+  if (absmax) block_max_to(mb, absmax);
+}
+
+// multigrid3d._sweep_rhs (multigrid3d.py:357-391).
+template <bool CTL>
+__global__ void __launch_bounds__(kThreads)
+k_sweep_rhs(double* __restrict__ e, const uint8_t* __restrict__ fixed,
+            const double* __restrict__ f, SweepGeom g, double omega,
+            int colour, unsigned long long* dslot, PairCtl* ctl, int lp) {
+  if (CTL) {
+    if (pair_skip(ctl, colour, lp)) return;
+    dslot = &ctl->slot[2 * lp + colour];
+  }
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  unsigned long long mb = 0;
+  if (t < g.total) {
+    const uint32_t ij = fdiv(t, g.div_kk);
+    const uint32_t kk = t - ij * g.div_kk.d;
+    const uint32_t i = fdiv(ij, g.div_ny);
+    const uint32_t j = ij - i * g.div_ny.d;
+    const long k = 2 * (long)kk + ((i + j + colour) & 1);
+    if (k < g.nz) {
+      const size_t p = ((size_t)i * g.ny + j) * g.nz + k;
+      if (!fixed[p]) {
+        const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
+        double v[6];
+        load6(e, n, v);
+        const double old = e[p];
+        const double nv = div6(__dsub_rn(sum6(v), f[p]));
+        const double nw = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(nv, old)));
+        mb = absbits(__dsub_rn(nw, old));
+        e[p] = nw;
+      }
+    }
+  }
+  block_max_to(mb, dslot);
+}
+
+// multigrid3d._residual_rhs (multigrid3d.py:394-417).
+__global__ void __launch_bounds__(kThreads)
+k_residual_rhs(const double* __restrict__ e, const uint8_t* __restrict__ fixed,
+               const double* __restrict__ f, FlatGeom g,
+               double* __restrict__ out) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= g.total) return;
+  const uint32_t ij = fdiv(t, g.div_nz);
+  const uint32_t k = t - ij * g.div_nz.d;
+  const uint32_t i = fdiv(ij, g.div_ny);
+  const uint32_t j = ij - i * g.div_ny.d;
+  double r = 0.0;
+  if (!fixed[t]) {
+    const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
+    double v[6];
+    load6(e, n, v);
+    r = __dsub_rn(__dsub_rn(sum6(v), __dmul_rn(6.0, e[t])), f[t]);
+  }
+  out[t] = r;
+}
+
+// multigrid3d._restrict_fw_njit (multigrid3d.py:420-455).
+__global__ void __launch_bounds__(kThreads)
+k_restrict(const double* __restrict__ fine, long nx, long ny, long nz,
+           double* __restrict__ out, FlatGeom c, int neg4) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= c.total) return;
+  const uint32_t ij = fdiv(t, c.div_nz);
+  const long kc = t - ij * c.div_nz.d;
+  const long ic = fdiv(ij, c.div_ny);
+  const long jc = ij - ic * c.div_ny.d;
+  const long i = 2 * ic, j = 2 * jc, k = 2 * kc;
+  double acc = 0.0;
+#pragma unroll
+  for (int di = -1; di <= 1; di++) {
+    long ii = i + di;
+    ii = ii < 0 ? 0 : (ii > nx - 1 ? nx - 1 : ii);
+    const double wi = di == 0 ? 1.0 : 0.5;
+#pragma unroll
+    for (int dj = -1; dj <= 1; dj++) {
+      long jj = j + dj;
+      jj = jj < 0 ? 0 : (jj > ny - 1 ? ny - 1 : jj);
+      const double wj = dj == 0 ? 1.0 : 0.5;
+      const double* row = fine + ((size_t)ii * ny + jj) * nz;
+#pragma unroll
+      for (int dk = -1; dk <= 1; dk++) {
+        long kk = k + dk;
+        kk = kk < 0 ? 0 : (kk > nz - 1 ? nz - 1 : kk);
+        const double wk = dk == 0 ? 1.0 : 0.5;
+        // wi*wj*wk is a power of two, folded at compile time
+        acc = __dadd_rn(acc, __dmul_rn(wi * wj * wk, row[kk]));
+      }
+    }
+  }
+  double r = __dmul_rn(acc, 0.125);  // == acc / 8.0 (power-of-two scale)
+  if (neg4) r = -__dmul_rn(r, 4.0);
+  out[t] = r;
+}
+
+struct Lerp {
+  long a0, a1;
+  double t;
+};
+
+// multigrid3d.py:465-481 (prolong-add coordinates)
+__device__ __forceinline__ Lerp pa_axis(long i, long c) {
+  double xf = __dmul_rn((double)i, 0.5);
+  if (xf > (double)(c - 1)) xf = (double)c - 1.0;
+  long x0 = (long)xf;
+  if (x0 > c - 2) x0 = c > 1 ? c - 2 : 0;
+  Lerp l;
+  l.a0 = x0;
+  l.a1 = c > 1 ? x0 + 1 : x0;
+  l.t = __dsub_rn(xf, (double)x0);
+  return l;
+}
+
+// multigrid3d.py:144-156 (cascadic prolongation coordinates)
+__device__ __forceinline__ Lerp pl_axis(long i, long c) {
+  double xf = __ddiv_rn((double)i, 2.0);
+  if (xf > (double)(c - 1)) xf = (double)(c - 1);
+  const long x0 = (long)floor(xf);
+  Lerp l;
+  l.a0 = x0;
+  l.a1 = x0 + 1 < c - 1 ? x0 + 1 : c - 1;
+  l.t = __dsub_rn(xf, (double)x0);
+  return l;
+}
+
+__device__ __forceinline__ double lerp_ref(double a, double b, double t) {
+  // a*(1-t) + b*t, evaluated as the reference writes it
+  return __dadd_rn(__dmul_rn(a, __dsub_rn(1.0, t)), __dmul_rn(b, t));
+}
+
+__device__ __forceinline__ double trilinear(const double* __restrict__ c,
+                                            long cy, long cz, const Lerp& x,
+                                            const Lerp& y, const Lerp& z) {
+#define C(a, b, d) c[((size_t)(a) * cy + (b)) * cz + (d)]
+  const double c00 = lerp_ref(C(x.a0, y.a0, z.a0), C(x.a1, y.a0, z.a0), x.t);
+  const double c10 = lerp_ref(C(x.a0, y.a1, z.a0), C(x.a1, y.a1, z.a0), x.t);
+  const double c01 = lerp_ref(C(x.a0, y.a0, z.a1), C(x.a1, y.a0, z.a1), x.t);
+  const double c11 = lerp_ref(C(x.a0, y.a1, z.a1), C(x.a1, y.a1, z.a1), x.t);
+#undef C
+  const double c0 = lerp_ref(c00, c10, y.t);
+  const double c1 = lerp_ref(c01, c11, y.t);
+  return lerp_ref(c0, c1, z.t);
+}
+
+// multigrid3d._prolong_add_njit (multigrid3d.py:458-499).
+__global__ void __launch_bounds__(kThreads)
+k_prolong_add(const double* __restrict__ coarse, long cx, long cy, long cz,
+              double* __restrict__ out, const uint8_t* __restrict__ fixed,
+              FlatGeom g) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= g.total) return;
+  if (fixed[t]) return;
+  const uint32_t ij = fdiv(t, g.div_nz);
+  const long k = t - ij * g.div_nz.d;
+  const long i = fdiv(ij, g.div_ny);
+  const long j = ij - i * g.div_ny.d;
+  const Lerp x = pa_axis(i, cx), y = pa_axis(j, cy), z = pa_axis(k, cz);
+  out[t] = __dadd_rn(out[t], trilinear(coarse, cy, cz, x, y, z));
+}
+
+// multigrid3d._prolongate (multigrid3d.py:138-171).
+__global__ void __launch_bounds__(kThreads)
+k_prolongate(const double* __restrict__ coarse, long cx, long cy, long cz,
+             double* __restrict__ out, FlatGeom g) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= g.total) return;
+  const uint32_t ij = fdiv(t, g.div_nz);
+  const long k = t - ij * g.div_nz.d;
+  const long i = fdiv(ij, g.div_ny);
+  const long j = ij - i * g.div_ny.d;
+  const Lerp x = pl_axis(i, cx), y = pl_axis(j, cy), z = pl_axis(k, cz);
+  out[t] = trilinear(coarse, cy, cz, x, y, z);
+}
+
+// multigrid3d._coarsen_fixed_any (multigrid3d.py:507-526).
+__global__ void __launch_bounds__(kThreads)
+k_coarsen_any(const uint8_t* __restrict__ fixed, long nx, long ny, long nz,
+              uint8_t* __restrict__ out, FlatGeom c) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= c.total) return;
+  const uint32_t ij = fdiv(t, c.div_nz);
+  const long kc = t - ij * c.div_nz.d;
+  const long ic = fdiv(ij, c.div_ny);
+  const long jc = ij - ic * c.div_ny.d;
+  uint8_t any = 0;
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++)
+      for (int q = 0; q < 2; q++) {
+        const long i = 2 * ic + a, j = 2 * jc + b, k = 2 * kc + q;
+        if (i < nx && j < ny && k < nz && fixed[((size_t)i * ny + j) * nz + k]) any = 1;
+      }
+  out[t] = any;
+}
+
+// multigrid3d._coarsen_mask (multigrid3d.py:85-135).
+__global__ void __launch_bounds__(kThreads)
+k_coarsen_mask(const uint8_t* __restrict__ fixed, const double* __restrict__ val,
+               long nx, long ny, long nz, uint8_t* __restrict__ fc,
+               double* __restrict__ vc, FlatGeom c) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= c.total) return;
+  const uint32_t ij = fdiv(t, c.div_nz);
+  const long kc = t - ij * c.div_nz.d;
+  const long ic = fdiv(ij, c.div_ny);
+  const long jc = ij - ic * c.div_ny.d;
+  const size_t p0 = ((size_t)(2 * ic) * ny + 2 * jc) * nz + 2 * kc;
+  if (fixed[p0]) {
+    fc[t] = 1;
+    vc[t] = val[p0];
+    return;
+  }
+  unsigned long long best = 0;
+  bool any = false;
+  double bv = 0.0;
+  for (int a = 0; a < 2; a++)
+    for (int b = 0; b < 2; b++)
+      for (int q = 0; q < 2; q++) {
+        const long i = 2 * ic + a, j = 2 * jc + b, k = 2 * kc + q;
+        if (i >= nx || j >= ny || k >= nz) continue;
+        const size_t p = ((size_t)i * ny + j) * nz + k;
+        if (!fixed[p]) continue;
+        const double v = val[p];
+        // |v| compared through its bits (first maximum wins, as argmax)
+        const unsigned long long m =
+            (static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7fffffffffffffffULL) + 1ULL;
+        if (!any || m > best) {
+          best = m;
+          bv = v;
+        }
+        any = true;
+      }
+  fc[t] = any ? 1 : 0;
+  vc[t] = any ? bv : val[p0];
+}
+
+__global__ void k_set_fixed(double* __restrict__ phi,
+                            const uint8_t* __restrict__ fixed,
+                            const double* __restrict__ val, size_t n) {
+  const size_t t = (size_t)blockIdx.x * kThreads + threadIdx.x;
+  if (t < n && fixed[t]) phi[t] = val[t];
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_absdiff_max(const double* __restrict__ a, const double* __restrict__ b,
+              size_t n, unsigned long long* bits, int* nan_flag) {
+  unsigned long long mb = 0;
+  bool nan = false;
+  for (size_t t = (size_t)blockIdx.x * kThreads + threadIdx.x; t < n;
+       t += (size_t)gridDim.x * kThreads) {
+    const double d = b ? __dsub_rn(a[t], b[t]) : a[t];
+    const unsigned long long x =
+        static_cast<unsigned long long>(__double_as_longlong(d)) & 0x7fffffffffffffffULL;
+    if (x > 0x7ff0000000000000ULL) nan = true;
+    else if (x > mb) mb = x;
+  }
+  if (__syncthreads_or(nan) && threadIdx.x == 0) *nan_flag = 1;
+  block_max_to(mb, bits);
+}
+
+// phi <- (phi + flip(phi, axis)) * 0.5 (multigrid3d.py:689-691); each thread
+// owns a mirror pair, so the in-place update reads both values first.
+__global__ void __launch_bounds__(kThreads)
+k_sym_project(double* __restrict__ phi, FlatGeom g, int axis) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= g.total) return;
+  const uint32_t ij = fdiv(t, g.div_nz);
+  const long k = t - ij * g.div_nz.d;
+  const long i = fdiv(ij, g.div_ny);
+  const long j = ij - i * g.div_ny.d;
+  long mi = i, mj = j, mk = k;
+  if (axis == 0) mi = g.nx - 1 - i;
+  else if (axis == 1) mj = g.ny - 1 - j;
+  else mk = g.nz - 1 - k;
+  const size_t q = ((size_t)mi * g.ny + mj) * g.nz + mk;
+  if (q < t) return;  // the partner with the lower index does the pair
+  const double s = __dmul_rn(__dadd_rn(phi[t], phi[q]), 0.5);
+  phi[t] = s;
+  phi[q] = s;
+}
+
+// solver3d._residual_kernel (solver3d.py:366-386): num/den - u.
+__global__ void __launch_bounds__(kThreads)
+k_residual_audit(const double* __restrict__ u, const uint8_t* __restrict__ fixed,
+                 const float* __restrict__ th, FlatGeom g,
+                 double* __restrict__ out) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= g.total) return;
+  const uint32_t ij = fdiv(t, g.div_nz);
+  const uint32_t k = t - ij * g.div_nz.d;
+  const uint32_t i = fdiv(ij, g.div_ny);
+  const uint32_t j = ij - i * g.div_ny.d;
+  double r = 0.0;
+  if (!fixed[t]) {
+    const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
+    double v[6], num, den;
+    load6(u, n, v);
+    theta_num_den<kThetaGhost>(v, th, g.total, t, num, den);
+    r = __dsub_rn(__ddiv_rn(num, den), u[t]);
+  }
+  out[t] = r;
+}
+
+// solver3d._err_sweep (solver3d.py:389-417).
+__global__ void __launch_bounds__(kThreads)
+k_err_sweep(double* __restrict__ e, const uint8_t* __restrict__ fixed,
+            const float* __restrict__ th, const double* __restrict__ rhs,
+            SweepGeom g, double omega, int colour, unsigned long long* dslot) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  unsigned long long mb = 0;
+  if (t < g.total) {
+    const uint32_t ij = fdiv(t, g.div_kk);
+    const uint32_t kk = t - ij * g.div_kk.d;
+    const uint32_t i = fdiv(ij, g.div_ny);
+    const uint32_t j = ij - i * g.div_ny.d;
+    const long k = 2 * (long)kk + ((i + j + colour) & 1);
+    if (k < g.nz) {
+      const size_t p = ((size_t)i * g.ny + j) * g.nz + k;
+      if (!fixed[p]) {
+        const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
+        double v[6], num, den;
+        load6(e, n, v);
+        theta_num_den<kThetaGhost>(v, th, (size_t)g.nx * g.ny * g.nz, p, num, den);
+        const double old = e[p];
+        const double inner = __dsub_rn(__dadd_rn(__ddiv_rn(num, den), rhs[p]), old);
+        const double nw = __dadd_rn(old, __dmul_rn(omega, inner));
+        mb = absbits(__dsub_rn(nw, old));
+        e[p] = nw;
+      }
+    }
+  }
+  block_max_to(mb, dslot);
+}
+
+__global__ void k_fill_ones_f32(float* a, size_t n) {
+  const size_t t = (size_t)blockIdx.x * kThreads + threadIdx.x;
+  if (t < n) a[t] = 1.0f;
+}
+
+}  // namespace
+
+void launch_sweep(cudaStream_t s, double* phi, const uint8_t* fixed,
+                  const float* th, int kind, Dims d, double omega, int colour,
+                  unsigned long long* dslot, PairCtl* ctl, int lp) {
+  const SweepGeom g = sweep_geom(d);
+  const unsigned nb = blocks_for(g.total);
+  if (nb == 0) return;
+  counted();
+#define IG_SWEEP(K)                                                              \
+  if (ctl) k_sweep<K, true><<<nb, kThreads, 0, s>>>(phi, fixed, th, g, omega,    \
+                                                    colour, dslot, ctl, lp);     \
+  else k_sweep<K, false><<<nb, kThreads, 0, s>>>(phi, fixed, th, g, omega,       \
+                                                 colour, dslot, ctl, lp);
+  if (kind == kPlain) { IG_SWEEP(kPlain) }
+  else if (kind == kThetaGhost) { IG_SWEEP(kThetaGhost) }
+  else { IG_SWEEP(kThetaSW) }
+#undef IG_SWEEP
+}
+
+void launch_residual(cudaStream_t s, const double* phi, const uint8_t* fixed,
+                     const float* th, int kind, Dims d, double* out,
+                     unsigned long long* absmax) {
+  const FlatGeom g = flat_geom(d);
+  const unsigned nb = blocks_for(g.total);
+  if (nb == 0) return;
+  counted();
+  if (kind == kPlain)
+    k_residual<kPlain><<<nb, kThreads, 0, s>>>(phi, fixed, th, g, out, absmax);
+  else if (kind == kPlainSW)
+    k_residual<kPlainSW><<<nb, kThreads, 0, s>>>(phi, fixed, th, g, out, absmax);
+  else if (kind == kThetaGhost)
+    k_residual<kThetaGhost><<<nb, kThreads, 0, s>>>(phi, fixed, th, g, out, absmax);
+  else
+    k_residual<kThetaSW><<<nb, kThreads, 0, s>>>(phi, fixed, th, g, out, absmax);
+}
+
+void launch_sweep_rhs(cudaStream_t s, double* e, const uint8_t* fixed,
+                      const double* f, Dims d, double omega, int colour,
+                      unsigned long long* dslot, PairCtl* ctl, int lp) {
+  const SweepGeom g = sweep_geom(d);
+  const unsigned nb = blocks_for(g.total);
+  if (nb == 0) return;
+  counted();
+  if (ctl)
+    k_sweep_rhs<true><<<nb, kThreads, 0, s>>>(e, fixed, f, g, omega, colour, dslot, ctl, lp);
+  else
+    k_sweep_rhs<false><<<nb, kThreads, 0, s>>>(e, fixed, f, g, omega, colour, dslot, ctl, lp);
+}
+
+void launch_residual_rhs(cudaStream_t s, const double* e, const uint8_t* fixed,
+                         const double* f, Dims d, double* out) {
+  const FlatGeom g = flat_geom(d);
+  const unsigned nb = blocks_for(g.total);
+  if (nb) {
+    k_residual_rhs<<<nb, kThreads, 0, s>>>(e, fixed, f, g, out);
+    counted();
+  }
+}
+
+void launch_restrict(cudaStream_t s, const double* fine, Dims d, double* out,
+                     Dims c, int neg4) {
+  const FlatGeom g = flat_geom(c);
+  const unsigned nb = blocks_for(g.total);
+  if (nb) {
+    k_restrict<<<nb, kThreads, 0, s>>>(fine, d.nx, d.ny, d.nz, out, g, neg4);
+    counted();
+  }
+}
+
+void launch_prolong_add(cudaStream_t s, const double* coarse, Dims c,
+                        double* out, const uint8_t* fixed, Dims d) {
+  const FlatGeom g = flat_geom(d);
+  const unsigned nb = blocks_for(g.total);
+  if (nb) {
+    k_prolong_add<<<nb, kThreads, 0, s>>>(coarse, c.nx, c.ny, c.nz, out, fixed, g);
+    counted();
+  }
+}
+
+void launch_prolongate(cudaStream_t s, const double* coarse, Dims c,
+                       double* out, Dims d) {
+  const FlatGeom g = flat_geom(d);
+  const unsigned nb = blocks_for(g.total);
+  if (nb) {
+    k_prolongate<<<nb, kThreads, 0, s>>>(coarse, c.nx, c.ny, c.nz, out, g);
+    counted();
+  }
+}
+
+void launch_coarsen_any(cudaStream_t s, const uint8_t* fixed, Dims d,
+                        uint8_t* out, Dims c) {
+  const FlatGeom g = flat_geom(c);
+  const unsigned nb = blocks_for(g.total);
+  if (nb) {
+    k_coarsen_any<<<nb, kThreads, 0, s>>>(fixed, d.nx, d.ny, d.nz, out, g);
+    counted();
+  }
+}
+
+void launch_coarsen_mask(cudaStream_t s, const uint8_t* fixed,
+                         const double* val, Dims d, uint8_t* fc, double* vc,
+                         Dims c) {
+  const FlatGeom g = flat_geom(c);
+  const unsigned nb = blocks_for(g.total);
+  if (nb) {
+    k_coarsen_mask<<<nb, kThreads, 0, s>>>(fixed, val, d.nx, d.ny, d.nz, fc, vc, g);
+    counted();
+  }
+}
+
+void launch_set_fixed(cudaStream_t s, double* phi, const uint8_t* fixed,
+                      const double* val, size_t n) {
+  const unsigned nb = blocks_for(n);
+  if (nb) {
+    k_set_fixed<<<nb, kThreads, 0, s>>>(phi, fixed, val, n);
+    counted();
+  }
+}
+
+void launch_absdiff_max(cudaStream_t s, const double* a, const double* b,
+                        size_t n, unsigned long long* bits, int* nan_flag) {
+  unsigned nb = blocks_for(n);
+  if (nb > 152u * 8u) nb = 152u * 8u;
+  if (nb) {
+    k_absdiff_max<<<nb, kThreads, 0, s>>>(a, b, n, bits, nan_flag);
+    counted();
+  }
+}
+
+void launch_sym_project(cudaStream_t s, double* phi, Dims d, int axis) {
+  const FlatGeom g = flat_geom(d);
+  const unsigned nb = blocks_for(g.total);
+  if (nb) {
+    k_sym_project<<<nb, kThreads, 0, s>>>(phi, g, axis);
+    counted();
+  }
+}
+
+void launch_residual_audit(cudaStream_t s, const double* u,
+                           const uint8_t* fixed, const float* th, Dims d,
+                           double* out) {
+  const FlatGeom g = flat_geom(d);
+  const unsigned nb = blocks_for(g.total);
+  if (nb) {
+    k_residual_audit<<<nb, kThreads, 0, s>>>(u, fixed, th, g, out);
+    counted();
+  }
+}
+
+void launch_err_sweep(cudaStream_t s, double* e, const uint8_t* fixed,
+                      const float* th, const double* rhs, Dims d, double omega,
+                      int colour, unsigned long long* dslot) {
+  const SweepGeom g = sweep_geom(d);
+  const unsigned nb = blocks_for(g.total);
+  if (nb) {
+    k_err_sweep<<<nb, kThreads, 0, s>>>(e, fixed, th, rhs, g, omega, colour, dslot);
+    counted();
+  }
+}
+
+void launch_fill_ones_f32(cudaStream_t s, float* a, size_t n) {
+  const unsigned nb = blocks_for(n);
+  if (nb) {
+    k_fill_ones_f32<<<nb, kThreads, 0, s>>>(a, n);
+    counted();
+  }
+}
+
+}  // namespace ig

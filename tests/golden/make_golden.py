@@ -1,0 +1,395 @@
+"""Generate the golden fixtures under tests/golden/ by running the reference
+ion_gym solver itself (unmodified, from a checkout given by --ref) under the
+pure-Python numba stand-in in tests/golden/numba_stub.
+
+    PYTHONPATH=tests/golden/numba_stub:<ion_gym checkout> \
+        NUMBA_CACHE_DIR=/tmp/nbc ION_GYM_CACHE=/tmp/igc \
+        python tests/golden/make_golden.py
+
+Nothing in the test-suite or the library imports the reference at run time:
+the fixtures written here are the only thing carried forward.  Every case
+stores its inputs, the exact call, and the reference's outputs, so a test can
+replay the call through the oracle or the CUDA path and compare bits.
+
+Fixture files:
+  kernels.npz  single calls of the reference's numba kernels
+               (solver3d._sweep, multigrid3d._residual, _sweep_rhs,
+               _residual_rhs, _restrict_fw_njit, _prolong_add_njit,
+               _coarsen_fixed_any, _coarsen_mask, _prolongate,
+               solver3d._residual_kernel, _err_sweep)
+  drivers.npz  whole solves (solve3d, solve3d_mg, solve3d_vmg, solve_bases,
+               solve_bases_mg) with their returned (phi, sweeps, delta) and
+               the messages of the refusals.
+"""
+import argparse
+import os
+import sys
+import time
+
+import numpy as np
+
+SHAPES = [(9, 10, 11), (8, 8, 8), (5, 6, 1), (1, 7, 9), (2, 3, 4),
+          (1, 1, 5), (3, 1, 1), (6, 5, 7)]
+
+
+def _theta(rng, shape, frac_ones=0.6, lo=1e-3):
+    th = rng.uniform(lo, 1.0, (6,) + shape).astype(np.float32)
+    th[rng.random(th.shape) < frac_ones] = 1.0
+    return th
+
+
+def kernel_cases(rng, S, M):
+    out = {}
+
+    def put(kind, idx, **arrs):
+        for k, v in arrs.items():
+            out[f"{kind}/{idx}/{k}"] = np.asarray(v)
+
+    # _sweep ---------------------------------------------------------------
+    variants = [(False, True, 0, 1.83), (False, False, 1, 1.0),
+                (True, True, 1, 1.5), (True, False, 0, 1.2)]
+    idx = 0
+    for shape in SHAPES:
+        for use_th, gl, colour, omega in variants:
+            phi = rng.uniform(-2.0, 2.0, shape)
+            fixed = rng.random(shape) < 0.25
+            th = _theta(rng, shape) if use_th else np.ones((6,) + shape,
+                                                           np.float32)
+            p = phi.copy()
+            d = S._sweep(p, fixed, th, False, False, False, omega, colour, gl)
+            put("sweep", idx, phi=phi, fixed=fixed.astype(np.uint8), th=th,
+                has_theta=use_th, omega=omega, colour=colour, ghost_linear=gl,
+                out=p, d=float(d))
+            idx += 1
+
+    # multigrid _residual --------------------------------------------------
+    idx = 0
+    for shape in SHAPES:
+        for use_th, gl in [(False, True), (True, True), (True, False)]:
+            phi = rng.uniform(-2.0, 2.0, shape)
+            fixed = rng.random(shape) < 0.25
+            th = _theta(rng, shape) if use_th else np.ones((6,) + shape,
+                                                           np.float32)
+            r = np.full(shape, np.nan)
+            M._residual(phi, fixed, th, gl, r)
+            put("residual", idx, phi=phi, fixed=fixed.astype(np.uint8), th=th,
+                has_theta=use_th, ghost_linear=gl, out=r)
+            idx += 1
+
+    # _sweep_rhs / _residual_rhs -------------------------------------------
+    idx = 0
+    for shape in SHAPES:
+        for colour, omega in [(0, 1.0), (1, 1.0), (0, 1.71), (1, 1.71)]:
+            e = rng.uniform(-1.0, 1.0, shape)
+            f = rng.uniform(-3.0, 3.0, shape)
+            fixed = rng.random(shape) < 0.25
+            e[fixed] = 0.0
+            p = e.copy()
+            d = M._sweep_rhs(p, fixed, f, omega, colour)
+            r = np.full(shape, np.nan)
+            M._residual_rhs(e, fixed, f, r)
+            put("sweep_rhs", idx, e=e, f=f, fixed=fixed.astype(np.uint8),
+                omega=omega, colour=colour, out=p, d=float(d), res=r)
+            idx += 1
+
+    # _restrict_fw_njit, _coarsen_fixed_any, _coarsen_mask ------------------
+    idx = 0
+    for shape in SHAPES + [(3, 3, 3), (4, 5, 6)]:
+        fine = rng.uniform(-1.0, 1.0, shape)
+        cs = tuple((s + 1) // 2 for s in shape)
+        rc = np.full(cs, np.nan)
+        M._restrict_fw_njit(fine, rc)
+        fixed = rng.random(shape) < 0.15
+        val = np.where(fixed, rng.uniform(-5, 5, shape), rng.uniform(-1, 1, shape))
+        fa = M._coarsen_fixed_any(fixed)
+        fc, vc = M._coarsen_mask(fixed, val)
+        put("restrict", idx, fine=fine, out=rc, fixed=fixed.astype(np.uint8),
+            val=val, any=fa.astype(np.uint8), fc=fc.astype(np.uint8), vc=vc)
+        idx += 1
+
+    # _prolong_add_njit and cascadic _prolongate ---------------------------
+    idx = 0
+    for shape in SHAPES + [(3, 3, 3), (4, 5, 6)]:
+        cs = tuple((s + 1) // 2 for s in shape)
+        coarse = rng.uniform(-1.0, 1.0, cs)
+        base = rng.uniform(-1.0, 1.0, shape)
+        fixed = rng.random(shape) < 0.2
+        o = base.copy()
+        M._prolong_add_njit(coarse, o, fixed)
+        pl = M._prolongate(coarse, shape)
+        put("prolong", idx, coarse=coarse, base=base,
+            fixed=fixed.astype(np.uint8), out=o, prolongate=pl)
+        idx += 1
+
+    # solver3d audit kernels (_residual_kernel, _err_sweep) -----------------
+    idx = 0
+    for shape in [(9, 10, 11), (8, 8, 8), (6, 5, 7), (4, 5, 6)]:
+        u = rng.uniform(-2.0, 2.0, shape)
+        fixed = rng.random(shape) < 0.2
+        th = _theta(rng, shape)
+        r = S._residual_kernel(u, fixed, th)
+        e = rng.uniform(-0.1, 0.1, shape)
+        rhs = rng.uniform(-0.1, 0.1, shape)
+        p = e.copy()
+        d = S._err_sweep(p, fixed, th, rhs, 1.6, idx & 1)
+        put("audit", idx, u=u, fixed=fixed.astype(np.uint8), th=th, res=r,
+            e=e, rhs=rhs, omega=1.6, colour=idx & 1, out=p, d=float(d))
+        idx += 1
+    return out
+
+
+# ---------------------------------------------------------------- drivers
+def _sphere_box(shape, c, r, v=1.0):
+    i, j, k = np.meshgrid(*[np.arange(s, dtype=float) for s in shape],
+                          indexing="ij")
+    fixed = np.zeros(shape, bool)
+    fixed[0] = fixed[-1] = True
+    fixed[:, 0] = fixed[:, -1] = True
+    fixed[:, :, 0] = fixed[:, :, -1] = True
+    sph = (i - c[0]) ** 2 + (j - c[1]) ** 2 + (k - c[2]) ** 2 <= r * r
+    fixed |= sph
+    val = np.where(sph, v, 0.0)
+    return fixed, val
+
+
+def _plate(shape, thin=False):
+    nx, ny, nz = shape
+    fixed = np.zeros(shape, bool)
+    val = np.zeros(shape)
+    w = 1 if thin else 3
+    fixed[nx // 4:3 * nx // 4, ny // 2:ny // 2 + w, nz // 4:3 * nz // 4] = True
+    val[fixed] = 1e4
+    fixed[:, 0, :] = True
+    fixed[:, -1, :] = True
+    return fixed, val
+
+
+def driver_cases(rng, S, M):
+    out = {}
+
+    def put(kind, idx, **arrs):
+        for k, v in arrs.items():
+            out[f"{kind}/{idx}/{k}"] = np.asarray(v)
+
+    def timed(label, fn):
+        t = time.time()
+        r = fn()
+        print(f"  {label}: {time.time() - t:.1f}s", flush=True)
+        return r
+
+    # solve3d ---------------------------------------------------------------
+    cases = []
+    f, v = _sphere_box((12, 13, 11), (6, 6.5, 5), 2.6)
+    cases.append(dict(fixed=f, val=v, tol=1e-8, omega=None, phi0=None,
+                      theta=None, stencil="ghost_linear"))
+    phi0 = rng.uniform(0, 1, f.shape)
+    cases.append(dict(fixed=f, val=v, tol=1e-7, omega=1.7, phi0=phi0,
+                      theta=None, stencil="ghost_linear"))
+    th = _theta(rng, f.shape, 0.8)
+    cases.append(dict(fixed=f, val=v, tol=1e-7, omega=None, phi0=None,
+                      theta=th, stencil="sw"))
+    cases.append(dict(fixed=f, val=v, tol=1e-7, omega=None, phi0=None,
+                      theta=th, stencil="ghost_linear"))
+    f1 = np.zeros((20, 17, 1), bool)
+    f1[0] = f1[-1] = True
+    f1[:, 0] = f1[:, -1] = True
+    f1[12:15, 5:8] = True
+    v1 = np.where(f1, 0.0, 0.0)
+    v1[12:15, 5:8] = 1e4
+    cases.append(dict(fixed=f1, val=v1, tol=1e-8, omega=1.0, phi0=None,
+                      theta=None, stencil="ghost_linear"))
+    for idx, c in enumerate(cases):
+        phi, sw, d = timed(f"solve3d {idx}", lambda: S.solve3d(
+            c["fixed"], c["val"], theta=c["theta"], tol=c["tol"],
+            omega=c["omega"], phi0=c["phi0"], stencil=c["stencil"]))
+        om = c["omega"] if c["omega"] is not None else S.optimal_omega(
+            c["fixed"].shape)
+        put("solve3d", idx, fixed=c["fixed"].astype(np.uint8), val=c["val"],
+            tol=c["tol"], omega=om, omega_given=c["omega"] is not None,
+            has_phi0=c["phi0"] is not None,
+            phi0=c["phi0"] if c["phi0"] is not None else np.zeros(0),
+            has_theta=c["theta"] is not None,
+            theta=c["theta"] if c["theta"] is not None else np.zeros(0,
+                                                                 np.float32),
+            stencil=c["stencil"], phi=phi, sweeps=sw, delta=d)
+    # the refusal
+    try:
+        S.solve3d(cases[0]["fixed"], cases[0]["val"], tol=1e-12,
+                  max_sweeps=7)
+        raise AssertionError("reference did not refuse")
+    except S.SolveNotConverged as e:
+        put("solve3d_refuse", 0, message=str(e))
+
+    # cascadic solve3d_mg ----------------------------------------------------
+    f, v = _sphere_box((21, 19, 23), (10, 9, 11), 4.2)
+    phi, sw, d = timed("solve3d_mg 0", lambda: M.solve3d_mg(f, v, tol=1e-8))
+    put("mg", 0, fixed=f.astype(np.uint8), val=v, tol=1e-8, max_levels=8,
+        has_theta=False, theta=np.zeros(0, np.float32), stencil="ghost_linear",
+        phi=phi, sweeps=sw, delta=d)
+    th = _theta(rng, f.shape, 0.85)
+    phi, sw, d = timed("solve3d_mg 1", lambda: M.solve3d_mg(
+        f, v, theta=th, tol=1e-7, max_levels=2, stencil="sw"))
+    put("mg", 1, fixed=f.astype(np.uint8), val=v, tol=1e-7, max_levels=2,
+        has_theta=True, theta=th, stencil="sw", phi=phi, sweeps=sw, delta=d)
+
+    # V-cycle solve3d_vmg -----------------------------------------------------
+    vcases = []
+    f, v = _plate((19, 21, 17))
+    vcases.append(dict(fixed=f, val=v, tol=1e-5, theta=None,
+                       stencil="ghost_linear", phi0=None))
+    f2, v2 = _plate((25, 27, 23), thin=True)
+    vcases.append(dict(fixed=f2, val=v2, tol=1e-5, theta=None,
+                       stencil="ghost_linear", phi0=None))
+    # x- and y-symmetric: exercises the symmetric-subspace projection
+    fs = np.zeros((21, 21, 15), bool)
+    fs[0] = fs[-1] = True
+    fs[:, 0] = fs[:, -1] = True
+    fs[7:14, 7:14, 5:10] = True
+    vs = np.where(fs, 0.0, 0.0)
+    vs[7:14, 7:14, 5:10] = 100.0
+    vcases.append(dict(fixed=fs, val=vs, tol=1e-7, theta=None,
+                       stencil="ghost_linear", phi0=None))
+    th = _theta(rng, f.shape, 0.95, lo=0.3)
+    vcases.append(dict(fixed=f, val=v, tol=1e-5, theta=th, stencil="sw",
+                       phi0=rng.uniform(0, 1e3, f.shape)))
+    for idx, c in enumerate(vcases):
+        phi, sw, d = timed(f"solve3d_vmg {idx}", lambda: M.solve3d_vmg(
+            c["fixed"], c["val"], theta=c["theta"], tol=c["tol"],
+            stencil=c["stencil"], phi0=c["phi0"]))
+        put("vmg", idx, fixed=c["fixed"].astype(np.uint8), val=c["val"],
+            tol=c["tol"], has_theta=c["theta"] is not None,
+            theta=c["theta"] if c["theta"] is not None else np.zeros(
+                0, np.float32),
+            stencil=c["stencil"], has_phi0=c["phi0"] is not None,
+            phi0=c["phi0"] if c["phi0"] is not None else np.zeros(0),
+            phi=phi, sweeps=sw, delta=d)
+    # refusals: cycle cap and stagnation (reference test_multigrid_refusal)
+    fp = np.zeros((20, 20, 20), bool)
+    vp = np.zeros((20, 20, 20))
+    fp[0] = fp[-1] = True
+    vp[0] = 100.0
+    try:
+        M.solve3d_vmg(fp, vp, tol=1e-30, max_cycles=1)
+        raise AssertionError("no cap refusal")
+    except S.SolveNotConverged as e:
+        put("vmg_refuse", 0, message=str(e))
+    try:
+        timed("stagnation", lambda: M.solve3d_vmg(fp, vp, tol=1e-14,
+                                                  max_cycles=200))
+        raise AssertionError("no stagnation refusal")
+    except S.SolveNotConverged as e:
+        put("vmg_refuse", 1, message=str(e))
+    phi, sw, d = M.solve3d_vmg(fp, vp, tol=1e-14, max_cycles=200,
+                               accept_stagnation=True)
+    put("vmg_refuse", 2, phi=phi, sweeps=sw, delta=d)
+
+    # solve_bases (SOR) and solve_bases_mg (V-cycle) --------------------------
+    shape = (14, 12, 10)
+    m1 = np.zeros(shape, bool)
+    m1[0] = True
+    m2 = np.zeros(shape, bool)
+    m2[-1] = True
+    m3 = np.zeros(shape, bool)
+    m3[5:8, 4:7, 3:6] = True
+    masks = {1: m1, 2: m2, 4: m3}
+    b = timed("solve_bases", lambda: S.solve_bases(masks, tol=1e-6))
+    put("bases", 0, m1=m1.astype(np.uint8), m2=m2.astype(np.uint8),
+        m4=m3.astype(np.uint8), b1=b[1], b2=b[2], b4=b[4])
+    shape = (19, 17, 21)
+    mm1 = np.zeros(shape, bool)
+    mm1[:, 0, :] = True
+    mm2 = np.zeros(shape, bool)
+    mm2[6:12, 8:10, 5:16] = True
+    mm3 = np.zeros(shape, bool)
+    mm3[:, -1, :] = True
+    masks = {1: mm1, 2: mm2, 3: mm3}
+    bm = timed("solve_bases_mg", lambda: M.solve_bases_mg(masks, tol=1e-4,
+                                                         only={1, 2}))
+    put("bases_mg", 0, m1=mm1.astype(np.uint8), m2=mm2.astype(np.uint8),
+        m3=mm3.astype(np.uint8), tol=1e-4, b1=bm[1], b2=bm[2],
+        keys=np.array(sorted(bm)))
+    return out
+
+
+def theta_cases(S):
+    """solver3d.fractions_from_scene on small analytic scenes: a coax
+    (cylinder inside a ring), a box with a cylindrical hole, and a folded
+    (mirror x, y) quadrant."""
+    from ion_gym.physics.scene3d import (GeomScene, GridSpec, Electrode,
+                                         Shape, Cylinder, Box3D)
+    out = {}
+    n, nz = 23, 5
+    c = 11.0
+    ii, jj = np.meshgrid(np.arange(n, dtype=float), np.arange(n, dtype=float),
+                         indexing="ij")
+    rr = np.hypot(ii - c, jj - c)
+    metal = ((rr <= 4.3) | (rr >= 9.6))[:, :, None] & np.ones((1, 1, nz), bool)
+    sc = GeomScene(grid=GridSpec(n, n, nz), units="gu", electrodes=[
+        Electrode(1, "inner", [Shape([Cylinder(c, c, nz + 2.0, 4.3,
+                                               nz + 4.0)])]),
+        Electrode(2, "outer", [Shape(within=[Cylinder(c, c, nz + 2.0, 40.0,
+                                                      nz + 4.0)],
+                                     notin=[Cylinder(c, c, nz + 2.0, 9.6,
+                                                     nz + 4.0)])])])
+    out["theta/0/metal"] = metal.astype(np.uint8)
+    out["theta/0/mirror"] = np.array([False, False, False])
+    out["theta/0/th"] = S.fractions_from_scene(sc, metal)
+    # a box plate with a hole, in mm (scaled to gu by the scene)
+    shape = (17, 15, 13)
+    i, j, k = np.meshgrid(*[np.arange(s, dtype=float) for s in shape],
+                          indexing="ij")
+    plate = ((i >= 2.6) & (i <= 13.2) & (j >= 1.3) & (j <= 12.7)
+             & (k >= 5.2) & (k <= 7.4)
+             & ~((i - 8.0) ** 2 + (j - 7.0) ** 2 < 3.1 ** 2))
+    sc2 = GeomScene(grid=GridSpec(*shape, mm_per_gu=0.5), units="mm",
+                    electrodes=[Electrode(1, "plate", [Shape(
+                        within=[Box3D(1.3, 0.65, 2.6, 6.6, 6.35, 3.7)],
+                        notin=[Cylinder(4.0, 3.5, 4.0, 1.55, 3.0)])])])
+    out["theta/1/metal"] = plate.astype(np.uint8)
+    out["theta/1/mirror"] = np.array([False, False, False])
+    out["theta/1/th"] = S.fractions_from_scene(sc2, plate)
+    # folded quadrant with mirror planes at x = 0 and y = 0
+    q = 15
+    qi, qj = np.meshgrid(np.arange(q, dtype=float), np.arange(q, dtype=float),
+                         indexing="ij")
+    rq = np.hypot(qi, qj)
+    mq = ((rq <= 3.7) | (rq >= 12.2))[:, :, None] & np.ones((1, 1, 3), bool)
+    sc3 = GeomScene(grid=GridSpec(q, q, 3), units="gu", electrodes=[
+        Electrode(1, "rod", [Shape([Cylinder(0.0, 0.0, 9.0, 3.7, 20.0)])]),
+        Electrode(2, "can", [Shape(within=[Cylinder(0.0, 0.0, 9.0, 40.0,
+                                                    20.0)],
+                                   notin=[Cylinder(0.0, 0.0, 9.0, 12.2,
+                                                   20.0)])])])
+    out["theta/2/metal"] = mq.astype(np.uint8)
+    out["theta/2/mirror"] = np.array([True, True, False])
+    out["theta/2/th"] = S.fractions_from_scene(sc3, mq,
+                                               mirror=(True, True, False))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
+    ap.add_argument("--only", choices=["kernels", "drivers", "theta"],
+                    default=None)
+    a = ap.parse_args()
+    import ion_gym.physics.solver3d as S
+    import ion_gym.physics.multigrid3d as M
+    assert "stub" in sys.modules["numba"].__version__, "run under the stub"
+    if a.only in (None, "kernels"):
+        rng = np.random.default_rng(20261203)
+        np.savez_compressed(os.path.join(a.out, "kernels.npz"),
+                            **kernel_cases(rng, S, M))
+        print("kernels.npz written")
+    if a.only in (None, "drivers"):
+        rng = np.random.default_rng(777)
+        np.savez_compressed(os.path.join(a.out, "drivers.npz"),
+                            **driver_cases(rng, S, M))
+        print("drivers.npz written")
+    if a.only in (None, "theta"):
+        np.savez_compressed(os.path.join(a.out, "theta.npz"), **theta_cases(S))
+        print("theta.npz written")
+
+
+if __name__ == "__main__":
+    main()
