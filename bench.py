@@ -46,29 +46,8 @@ FP64_BYTES_PER_LUP = 17      # read phi 8 + write phi 8 + mask 1
 
 
 def quadrupole(n=N_SIDE, r0=R0):
-    """Grounded box with four z-rods: radius 1.148 r0, axes at r0 + radius
-    from the centre on +-x (+1 V) and +-y (-1 V)."""
-    c = (n - 1) / 2.0
-    rad = 1.148 * r0
-    off = r0 + rad
-    ii, jj = np.meshgrid(np.arange(n, dtype=float), np.arange(n, dtype=float),
-                         indexing="ij")
-    fixed2 = np.zeros((n, n), bool)
-    val2 = np.zeros((n, n))
-    for (dx, dy, v) in ((off, 0, 1.0), (-off, 0, 1.0), (0, off, -1.0),
-                        (0, -off, -1.0)):
-        rod = (ii - c - dx) ** 2 + (jj - c - dy) ** 2 <= rad * rad
-        fixed2 |= rod
-        val2[rod] = v
-    fixed = np.repeat(fixed2[:, :, None], n, axis=2)
-    val = np.repeat(val2[:, :, None], n, axis=2)
-    fixed[0] = fixed[-1] = True
-    fixed[:, 0] = fixed[:, -1] = True
-    fixed[:, :, 0] = fixed[:, :, -1] = True
-    val[0] = val[-1] = 0.0
-    val[:, 0] = val[:, -1] = 0.0
-    val[:, :, 0] = val[:, :, -1] = 0.0
-    return fixed, val
+    from ion_gym_gb300.workloads import quadrupole as q
+    return q(n, r0)
 
 
 def level_shapes():
@@ -121,7 +100,7 @@ class Clocks:
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
                  "sw_power_cap"]
         reasons = sorted({names[i] for r in rows for i in range(4)
-                          if "Active" in r[5 + i]})
+                          if r[5 + i].strip() == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None,
                 "reasons": reasons, "samples": len(rows)}
@@ -314,7 +293,7 @@ def run_ours(a):
 # LUPs of one solve of this workload (sum over levels of nodes x pairs); the
 # iterates are identical on every implementation (the GPU sweeps return the
 # reference's bits), so the count is a property of the workload.
-LUPS_PER_SOLVE = None
+LUPS_PER_SOLVE = 26187534900   # 1500 fine pairs + 600 coarse-level pairs
 
 
 def run_reference(a):

@@ -1,0 +1,53 @@
+"""Small, self-contained launches of one kernel for profiling (ncu) and
+timing: the arrays are built, a few launches run, the process exits.
+
+    python -m ion_gym_gb300.profile_case sweep_f64 --n 257 --pairs 4
+
+Cases:
+  sweep_f64   FP64 red-black sweep (k_sweep<kPlain>) on the 257^3
+              quadrupole, `pairs` red-black pairs, omega 1.85
+  mixed       the mixed-precision basis solve of the ring stack (if built)
+"""
+import argparse
+import ctypes
+import time
+
+import numpy as np
+
+
+def sweep_f64(n, pairs):
+    import torch
+    from ion_gym_gb300 import _lib
+    from ion_gym_gb300.workloads import quadrupole
+    fixed, val = quadrupole(n)
+    phi = torch.from_numpy(val.copy()).cuda()
+    fx = torch.from_numpy(fixed.view(np.uint8)).cuda()
+    L = _lib.lib()
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    d = ctypes.c_double(0.0)
+    t0 = time.perf_counter()
+    for _ in range(pairs):
+        for colour in (0, 1):
+            st = L.ig_sweep_dev(ctypes.c_void_p(phi.data_ptr()),
+                                ctypes.c_void_p(fx.data_ptr()), None,
+                                n, n, n, 1.85, colour, 0, ctypes.byref(d), s)
+            _lib.check(st, "ig_sweep_dev")
+    torch.cuda.synchronize()
+    el = time.perf_counter() - t0
+    print(f"sweep_f64 n={n}: {pairs} pairs in {el * 1e3:.2f} ms "
+          f"({n ** 3 * pairs / el / 1e9:.1f} GLUP/s incl. host syncs), "
+          f"last max|d| {d.value:.3e}")
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["sweep_f64"])
+    ap.add_argument("--n", type=int, default=257)
+    ap.add_argument("--pairs", type=int, default=4)
+    a = ap.parse_args()
+    if a.case == "sweep_f64":
+        sweep_f64(a.n, a.pairs)
+
+
+if __name__ == "__main__":
+    main()

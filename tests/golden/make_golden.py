@@ -367,10 +367,42 @@ def theta_cases(S):
     return out
 
 
+def cache_cases():
+    """io/fa_cache.store of a small basis set (the entry layout of
+    build_stl3d.py:919-924) into a scratch root: the key, meta.json and the
+    .npy bytes the reference writes."""
+    import json
+    import tempfile
+    from ion_gym.io import fa_cache
+    out = {}
+    rng = np.random.default_rng(4)
+    specs = [{"stl3d-v1_bases": "0123456789abcdef" * 4},
+             {"geometry": {"h": 0.1, "name": "einzel"}, "v": [1.5, 2.25e-7],
+              "n": 3}]
+    lab = np.zeros((6, 5, 4), np.uint8)
+    lab[1:3, 2:4, :] = 1
+    lab[4:, :, 1:3] = 2
+    arrays = {"basis_1": rng.random((6, 5, 4)).astype(np.float32),
+              "basis_2": rng.random((6, 5, 4)).astype(np.float32),
+              "labels": lab}
+    for idx, spec in enumerate(specs):
+        with tempfile.TemporaryDirectory() as root:
+            key = fa_cache.store(spec, arrays, root=root)
+            meta = open(os.path.join(root, key, "meta.json")).read()
+            out[f"cache/{idx}/spec"] = np.array(json.dumps(spec))
+            out[f"cache/{idx}/key"] = np.array(key)
+            out[f"cache/{idx}/meta"] = np.array(meta)
+            for name in arrays:
+                raw = open(os.path.join(root, key, name + ".npy"), "rb").read()
+                out[f"cache/{idx}/npy_{name}"] = np.frombuffer(raw, np.uint8)
+                out[f"cache/{idx}/arr_{name}"] = arrays[name]
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
-    ap.add_argument("--only", choices=["kernels", "drivers", "theta"],
+    ap.add_argument("--only", choices=["kernels", "drivers", "theta", "cache"],
                     default=None)
     a = ap.parse_args()
     import ion_gym.physics.solver3d as S
@@ -389,6 +421,9 @@ def main():
     if a.only in (None, "theta"):
         np.savez_compressed(os.path.join(a.out, "theta.npz"), **theta_cases(S))
         print("theta.npz written")
+    if a.only in (None, "cache"):
+        np.savez_compressed(os.path.join(a.out, "cache.npz"), **cache_cases())
+        print("cache.npz written")
 
 
 if __name__ == "__main__":

@@ -1,0 +1,153 @@
+"""Host-side logic of the drop-in, on the CPU: the theta builder and the
+cache layout against fixtures recorded from the reference, the SOR factor,
+the multigrid level shapes, the stop flag shared with the library, and the
+refusals that happen before any GPU work."""
+import json
+import os
+import tempfile
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, Golden
+from oracle import port
+
+
+def test_fractions_from_scene_matches_reference():
+    from ion_gym_gb300.physics import solver3d as S
+    from ion_gym_gb300.physics.scene3d import (GeomScene, GridSpec, Electrode,
+                                               Shape, Cylinder, Box3D)
+    g = Golden("theta.npz")
+    cases = g.cases("theta")
+    n, nz, c = 23, 5, 11.0
+    sc0 = GeomScene(grid=GridSpec(n, n, nz), units="gu", electrodes=[
+        Electrode(1, "inner", [Shape([Cylinder(c, c, nz + 2.0, 4.3,
+                                               nz + 4.0)])]),
+        Electrode(2, "outer", [Shape(within=[Cylinder(c, c, nz + 2.0, 40.0,
+                                                      nz + 4.0)],
+                                     notin=[Cylinder(c, c, nz + 2.0, 9.6,
+                                                     nz + 4.0)])])])
+    sc1 = GeomScene(grid=GridSpec(17, 15, 13, mm_per_gu=0.5), units="mm",
+                    electrodes=[Electrode(1, "plate", [Shape(
+                        within=[Box3D(1.3, 0.65, 2.6, 6.6, 6.35, 3.7)],
+                        notin=[Cylinder(4.0, 3.5, 4.0, 1.55, 3.0)])])])
+    sc2 = GeomScene(grid=GridSpec(15, 15, 3), units="gu", electrodes=[
+        Electrode(1, "rod", [Shape([Cylinder(0.0, 0.0, 9.0, 3.7, 20.0)])]),
+        Electrode(2, "can", [Shape(within=[Cylinder(0.0, 0.0, 9.0, 40.0,
+                                                    20.0)],
+                                   notin=[Cylinder(0.0, 0.0, 9.0, 12.2,
+                                                   20.0)])])])
+    for sc, case in zip((sc0, sc1, sc2), cases):
+        th = S.fractions_from_scene(sc, case["metal"].astype(bool),
+                                    mirror=tuple(bool(x) for x in
+                                                 case["mirror"]))
+        assert th.dtype == np.float32
+        assert np.array_equal(th, case["th"])
+        assert (th < 1).sum() > 0
+
+
+def test_cache_layout_matches_reference():
+    from ion_gym_gb300.io import fa_cache
+    g = Golden("cache.npz")
+    for c in g.cases("cache"):
+        spec = json.loads(str(c["spec"]))
+        assert fa_cache.spec_key(spec) == str(c["key"])
+        arrays = {k[4:]: c[k] for k in c if k.startswith("arr_")}
+        with tempfile.TemporaryDirectory() as root:
+            key = fa_cache.store(spec, arrays, root=root)
+            assert key == str(c["key"])
+            meta = json.load(open(os.path.join(root, key, "meta.json")))
+            assert meta == json.loads(str(c["meta"]))
+            for name in arrays:
+                raw = open(os.path.join(root, key, name + ".npy"), "rb").read()
+                assert raw == c[f"npy_{name}"].tobytes()
+            back, m2 = fa_cache.load(key, root=root)
+            for name, a in arrays.items():
+                assert np.array_equal(back[name], a)
+            # a tampered array is refused loudly, a missing entry is a miss
+            p = os.path.join(root, key, "basis_1.npy")
+            a = np.load(p)
+            a.flat[0] += 1
+            np.save(p, a)
+            with pytest.raises(IOError, match="head hash"):
+                fa_cache.load(key, root=root)
+            assert fa_cache.load("0" * 16, root=root) == (None, None)
+
+
+def test_store_bases_layout():
+    from ion_gym_gb300.io import fa_cache
+    m1 = np.zeros((4, 3, 2), bool)
+    m1[0] = True
+    m2 = np.zeros((4, 3, 2), bool)
+    m2[-1] = True
+    bases = {1: np.full((4, 3, 2), 0.5), 2: np.full((4, 3, 2), 0.25)}
+    with tempfile.TemporaryDirectory() as root:
+        key = fa_cache.store_bases({"k": 1}, bases, {1: m1, 2: m2}, root=root)
+        b, masks = fa_cache.load_bases(key, root=root)
+        assert b[1].dtype == np.float32 and np.all(b[1] == 0.5)
+        assert np.array_equal(masks[2], m2)
+        arrs, meta = fa_cache.load(key, root=root)
+        assert arrs["labels"].dtype == np.uint8
+        assert sorted(meta["arrays"]) == ["basis_1", "basis_2", "labels"]
+
+
+def test_optimal_omega_matches_restatement(drivers_golden):
+    from ion_gym_gb300.physics.solver3d import optimal_omega
+    for shape in [(65, 65, 65), (257,) * 3, (520, 80, 1), (1, 1, 1), (9, 10, 9),
+                  (193, 193, 385), (2, 2, 2)]:
+        assert optimal_omega(shape) == port.optimal_omega(shape)
+    assert optimal_omega((10, 20), spacing=(0.5, 1.0)) == \
+        port.optimal_omega((10, 20), spacing=(0.5, 1.0))
+    for c in drivers_golden.cases("solve3d"):
+        if not bool(c["omega_given"]):
+            assert optimal_omega(c["fixed"].shape) == float(c["omega"])
+
+
+def test_level_shapes():
+    from ion_gym_gb300.physics.multigrid3d import cascadic_shapes, bottom_shape
+    assert cascadic_shapes((257,) * 3, 9, 4) == [(257,) * 3, (129,) * 3,
+                                                 (65,) * 3, (33,) * 3]
+    assert cascadic_shapes((257,) * 3) == [(257,) * 3, (129,) * 3, (65,) * 3,
+                                           (33,) * 3, (17,) * 3, (9,) * 3]
+    assert cascadic_shapes((21, 19, 23)) == [(21, 19, 23), (11, 10, 12),
+                                             (6, 5, 6)]
+    assert cascadic_shapes((9, 50, 50)) == [(9, 50, 50)]
+    assert bottom_shape((193, 193, 385)) == (7, 7, 13)
+    assert bottom_shape((19, 21, 17)) == (10, 11, 9)
+    assert bottom_shape((5, 6, 1)) == (3, 3, 1)
+
+
+def test_stencil_refused_before_any_work():
+    from ion_gym_gb300.physics import solver3d as S, multigrid3d as M
+    f = np.zeros((4, 4, 4), bool)
+    for fn in (S.solve3d, M.solve3d_vmg, M.solve3d_mg):
+        with pytest.raises(ValueError, match="known stencils are"):
+            fn(f, np.zeros((4, 4, 4)), stencil="node")
+
+
+def test_stop_event_arms_the_library():
+    from ion_gym_gb300 import _lib
+    from ion_gym_gb300.physics import multigrid3d as M
+    L = _lib.lib()
+    M.clear_stop()
+    assert L.ig_stop_requested() == 0 and not M.stop_event().is_set()
+    M.request_stop()
+    assert L.ig_stop_requested() == 1 and M.stop_event().is_set()
+    M.stop_event().clear()
+    assert L.ig_stop_requested() == 0
+    M.stop_event().set()        # setting the event itself also arms it
+    assert L.ig_stop_requested() == 1
+    M.clear_stop()
+    assert isinstance(M.SOLVE_EXCLUSIVE, type(__import__("threading").Lock()))
+
+
+def test_no_gpu_means_a_loud_error():
+    """Without a device the solvers raise; nothing computes on the CPU."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    from ion_gym_gb300.physics import solver3d as S
+    f = np.zeros((5, 5, 5), bool)
+    f[0] = True
+    with pytest.raises(RuntimeError, match="no CUDA device"):
+        S.solve3d(f, np.where(f, 1.0, 0.0))
