@@ -132,6 +132,42 @@ int ig_cascadic_relres(const uint8_t *fixed, const double *val, long nx,
                        double *relres_out, long *total_pairs_out,
                        int *levels_out);
 
+/* Mixed-precision batched basis solve (the reference's solve_bases_mg
+ * problem, multigrid3d.py:233-291, with a different method and stopping
+ * rule): n_bases unit bases on the metal union `metal`, basis b at v_basis
+ * on masks[b] (n_bases stacked (nx,ny,nz) uint8 masks) and 0 on the rest of
+ * the metal.  FP32 red-black multigrid V-cycles (nu1/nu2 Gauss-Seidel pairs,
+ * `vcycles` per step) solve for the correction of the FP64 potential, whose
+ * FP64 residual is the reference's fine operator with theta None; a basis is
+ * done when one step changes its potential by less than `acc` (absolute,
+ * volts) anywhere.  Out: phi (n_bases x n float64), refinement steps, and
+ * each basis's last change.  IG_NOT_CONVERGED after max_steps. */
+int ig_mixed_bases(const uint8_t *metal, const uint8_t *masks, int n_bases,
+                   double v_basis, long nx, long ny, long nz, int stencil,
+                   double acc, int max_steps, int nu1, int nu2, int vcycles,
+                   double *phi_out, int *steps_out, double *dmax_out);
+
+/* Resident mixed-precision sessions (no reference counterpart): one
+ * geometry's multigrid hierarchy, potentials and captured CUDA graphs stay
+ * on the device between solves, on the session's own stream, so sessions of
+ * different geometries run concurrently.  ig_mixed_bytes: the device bytes a
+ * session for up to max_problems problems holds (admission by HBM
+ * footprint).  ig_mixed_solve_bases: as ig_mixed_bases on the session's
+ * metal.  ig_mixed_solve_values: n_problems Dirichlet problems on the
+ * session's metal, problem p with the values vals[p] (float64 (n) each) at
+ * the metal nodes.  Arrays may be host or device memory. */
+long ig_mixed_bytes(long nx, long ny, long nz, int max_problems);
+int ig_mixed_open(const uint8_t *metal, long nx, long ny, long nz,
+                  int max_problems, int stencil, int nu1, int nu2, int vcycles,
+                  void **handle);
+int ig_mixed_solve_bases(void *handle, const uint8_t *masks, int n_bases,
+                         double v_basis, double acc, int max_steps,
+                         double *phi_out, int *steps_out, double *dmax_out);
+int ig_mixed_solve_values(void *handle, const double *vals, int n_problems,
+                          double acc, int max_steps, double *phi_out,
+                          int *steps_out, double *dmax_out);
+void ig_mixed_close(void *handle);
+
 /* ---- single kernels on device arrays ----------------------------------- */
 
 /* solver3d._sweep (solver3d.py:131-198); theta NULL = all ones.  The max

@@ -64,6 +64,14 @@ SIGNATURES = {
     "ig_prof_reset": (None, []),
     "ig_prof_read": (None, [_pd, _pl, _pl]),
     "ig_launch_count": (_l, []),
+    "ig_mixed_bases": (_i, [_p, _p, _i, _d, _l, _l, _l, _i, _d, _i, _i, _i,
+                            _i, _p, _pi, _p]),
+    "ig_mixed_bytes": (_l, [_l, _l, _l, _i]),
+    "ig_mixed_open": (_i, [_p, _l, _l, _l, _i, _i, _i, _i, _i,
+                           ctypes.POINTER(ctypes.c_void_p)]),
+    "ig_mixed_solve_bases": (_i, [_p, _p, _i, _d, _d, _i, _p, _pi, _p]),
+    "ig_mixed_solve_values": (_i, [_p, _p, _i, _d, _i, _p, _pi, _p]),
+    "ig_mixed_close": (None, [_p]),
 }
 
 _lib = None

@@ -34,7 +34,11 @@ __host__ __device__ __forceinline__ long hi_nb(long i, long n) {
 // bit-for-bit against x/6.0 by the test-suite.
 __device__ __forceinline__ double div6(double x) {
   const unsigned e = (static_cast<unsigned>(__double2hiint(x)) >> 20) & 0x7ffu;
-  if (e < 64u || e > 2000u) return __ddiv_rn(x, 6.0);
+  if (e < 64u || e > 2000u) {
+    // +-0 / 6 is +-0 (sign kept): cold starts are mostly zeros
+    if ((static_cast<unsigned long long>(__double_as_longlong(x)) << 1) == 0ULL) return x;
+    return __ddiv_rn(x, 6.0);
+  }
   const double zh = 0x1.5555555555555p-3;
   const double zl = 0x1.5555555555555p-57;
   return __fma_rn(x, zh, __dmul_rn(x, zl));

@@ -4,6 +4,7 @@
 #pragma once
 #include <cstddef>
 #include <cstdint>
+#include <string>
 #include <cuda_runtime.h>
 
 namespace ig {
@@ -100,5 +101,8 @@ void launch_fill_ones_f32(cudaStream_t s, float* a, size_t n);
 
 // Number of kernel launches this library has issued since it was loaded.
 long launch_total();
+
+// Sets the calling thread's ig_last_error() message.
+void set_last_error(const std::string& m);
 
 }  // namespace ig

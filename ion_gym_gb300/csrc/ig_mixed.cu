@@ -1,0 +1,737 @@
+// ig_mixed.cu -- mixed-precision batched solves (FP32 multigrid inside FP64
+// iterative refinement) on sm_103a.
+//
+// Problem: B Dirichlet problems that share one metal mask (the electrode
+// bases of a deck, or B voltage sets on one geometry), each solved to an
+// absolute accuracy `acc` in the potential:
+//
+//   phi64 <- Dirichlet values                                  (FP64, HBM)
+//   repeat:  g32 = -(float) r64(phi64)      r64: the reference's fine-level
+//                                           residual (multigrid3d.py:305-354)
+//                                           in FP64, 0 at metal
+//            e32 = m V-cycles on  A e = g   (FP32, A e = sum(nbr e) - 6 e,
+//                                           block-ANY coarse masks, full
+//                                           weighting x4, trilinear
+//                                           prolongation, red-black GS)
+//            phi64 += e32;  stop when max|e32| < acc   (per basis)
+//
+// FP32 data live in a red-black split layout: colour c of row (i, j) holds
+// nodes k = 2m + ((i+j+c) & 1) at index m, so one colour's update reads the
+// other colour's rows contiguously (the z-neighbours are slots m-1+p, m+p of
+// the same row, the x/y-neighbours slot m of the adjacent rows) and writes
+// its own rows without touching the other colour: about 13 bytes per node
+// update in FP32 against 26 for the natural layout.
+//
+// Batching: blockIdx.y is the problem index; masks are shared, per-problem
+// arrays are strided.  The whole refinement step (residual, V-cycles,
+// update) is captured once into a CUDA graph and replayed; the host reads
+// only the B correction maxima per step.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+#include "ig_common.cuh"
+#include "ig_internal.h"
+#include "../../include/igsolve.h"
+
+namespace ig {
+namespace {
+
+constexpr int kT = 256;
+constexpr int kBottomMax = 1024;     // nodes of the coarsest level (one CTA)
+constexpr int kBottomThreads = 512;
+
+__device__ __forceinline__ uint32_t fdivu(uint32_t n, const FastDiv& f) {
+  return (__umulhi(n, f.m) + n) >> f.s;
+}
+
+// Geometry of one level in split layout.
+struct SGeo {
+  int nx, ny, nz, H;        // H = (nz + 1) / 2 slots per colour row
+  uint32_t csz;             // nx * ny * H (one colour array)
+  uint32_t n;               // nx * ny * nz (natural)
+  FastDiv dH, dny, dnz;
+};
+
+SGeo sgeo(const Dims& d) {
+  SGeo g;
+  g.nx = (int)d.nx;
+  g.ny = (int)d.ny;
+  g.nz = (int)d.nz;
+  g.H = (int)((d.nz + 1) / 2);
+  g.csz = (uint32_t)(d.nx * d.ny * g.H);
+  g.n = (uint32_t)d.n();
+  g.dH = FastDiv((uint32_t)g.H);
+  g.dny = FastDiv((uint32_t)d.ny);
+  g.dnz = FastDiv((uint32_t)d.nz);
+  return g;
+}
+
+__device__ __forceinline__ int lo_i(int i, int n) { return i > 0 ? i - 1 : (n > 1 ? 1 : i); }
+__device__ __forceinline__ int hi_i(int i, int n) { return i < n - 1 ? i + 1 : (n > 1 ? n - 2 : i); }
+
+// split index of natural node (i, j, k): colour and slot
+__device__ __forceinline__ uint32_t sidx(const SGeo& g, int i, int j, int k) {
+  return ((uint32_t)i * g.ny + j) * g.H + (k >> 1);
+}
+__device__ __forceinline__ int scol(int i, int j, int k) { return (i + j + k) & 1; }
+
+// Sum of the six neighbours of split slot (i, j, m) of colour c; own = own
+// colour array, oth = the other colour's array.  Size-1 axes use the node
+// itself (reference even-reflection rule, solver3d.py:156-167).
+__device__ __forceinline__ float nbr_sum(const SGeo& g, const float* __restrict__ own,
+                                         const float* __restrict__ oth, int i,
+                                         int j, int m, int k, uint32_t self) {
+  const float me = own[self];
+  const float xm = g.nx > 1 ? oth[((uint32_t)lo_i(i, g.nx) * g.ny + j) * g.H + m] : me;
+  const float xp = g.nx > 1 ? oth[((uint32_t)hi_i(i, g.nx) * g.ny + j) * g.H + m] : me;
+  const float ym = g.ny > 1 ? oth[((uint32_t)i * g.ny + lo_i(j, g.ny)) * g.H + m] : me;
+  const float yp = g.ny > 1 ? oth[((uint32_t)i * g.ny + hi_i(j, g.ny)) * g.H + m] : me;
+  float zm = me, zp = me;
+  if (g.nz > 1) {
+    const uint32_t row = ((uint32_t)i * g.ny + j) * g.H;
+    zm = oth[row + (lo_i(k, g.nz) >> 1)];
+    zp = oth[row + (hi_i(k, g.nz) >> 1)];
+  }
+  return ((xm + xp) + (ym + yp)) + (zm + zp);
+}
+
+// ---- FP32 kernels on split arrays (blockIdx.y = problem) ----------------
+
+// One red-black colour of Gauss-Seidel / SOR on A e = g.
+__global__ void __launch_bounds__(kT)
+k_gs(float* __restrict__ e, const float* __restrict__ g, const uint8_t* __restrict__ mask,
+     SGeo G, int c, float omega, size_t pstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= G.csz) return;
+  const uint32_t ij = fdivu(t, G.dH);
+  const int m = (int)(t - ij * G.dH.d);
+  const int i = (int)fdivu(ij, G.dny);
+  const int j = (int)(ij - (uint32_t)i * G.dny.d);
+  const int k = 2 * m + ((i + j + c) & 1);
+  if (k >= G.nz) return;
+  if (mask[(size_t)c * G.csz + t]) return;
+  float* eb = e + blockIdx.y * pstride;
+  const float* gb = g + blockIdx.y * pstride;
+  float* own = eb + (size_t)c * G.csz;
+  const float* oth = eb + (size_t)(1 - c) * G.csz;
+  const float s = nbr_sum(G, own, oth, i, j, m, k, t);
+  const float q = (s - gb[(size_t)c * G.csz + t]) * (1.0f / 6.0f);
+  own[t] = omega == 1.0f ? q : own[t] + omega * (q - own[t]);
+}
+
+// r = g - A e on natural layout (0 at metal).
+__global__ void __launch_bounds__(kT)
+k_resid(const float* __restrict__ e, const float* __restrict__ g,
+        const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ r,
+        size_t pstride, size_t rstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= G.n) return;
+  const uint32_t ij = fdivu(t, G.dnz);
+  const int k = (int)(t - ij * G.dnz.d);
+  const int i = (int)fdivu(ij, G.dny);
+  const int j = (int)(ij - (uint32_t)i * G.dny.d);
+  const int c = scol(i, j, k);
+  const uint32_t s = sidx(G, i, j, k);
+  float out = 0.f;
+  if (!mask[(size_t)c * G.csz + s]) {
+    const float* eb = e + blockIdx.y * pstride;
+    const float* own = eb + (size_t)c * G.csz;
+    const float* oth = eb + (size_t)(1 - c) * G.csz;
+    const float a = nbr_sum(G, own, oth, i, j, k >> 1, k, s) - 6.0f * own[s];
+    out = g[blockIdx.y * pstride + (size_t)c * G.csz + s] - a;
+  }
+  r[blockIdx.y * rstride + t] = out;
+}
+
+// Coarse right-hand side: 4 x full weighting of the fine residual
+// (27 points, weights 1/2 per off-centre step, clamped edges, /8), written
+// to the coarse split layout.
+__global__ void __launch_bounds__(kT)
+k_restrict(const float* __restrict__ r, SGeo F, float* __restrict__ gc, SGeo C,
+           size_t rstride, size_t cstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= C.n) return;
+  const uint32_t ij = fdivu(t, C.dnz);
+  const int kc = (int)(t - ij * C.dnz.d);
+  const int ic = (int)fdivu(ij, C.dny);
+  const int jc = (int)(ij - (uint32_t)ic * C.dny.d);
+  const float* rb = r + blockIdx.y * rstride;
+  float acc = 0.f;
+#pragma unroll
+  for (int di = -1; di <= 1; di++) {
+    const int ii = min(max(2 * ic + di, 0), F.nx - 1);
+    const float wi = di == 0 ? 1.f : 0.5f;
+#pragma unroll
+    for (int dj = -1; dj <= 1; dj++) {
+      const int jj = min(max(2 * jc + dj, 0), F.ny - 1);
+      const float wj = dj == 0 ? 1.f : 0.5f;
+      const float* row = rb + ((size_t)ii * F.ny + jj) * F.nz;
+      const float a = row[min(max(2 * kc - 1, 0), F.nz - 1)];
+      const float b = row[min(2 * kc, F.nz - 1)];
+      const float d = row[min(2 * kc + 1, F.nz - 1)];
+      acc += wi * wj * (0.5f * (a + d) + b);
+    }
+  }
+  const int c = scol(ic, jc, kc);
+  gc[blockIdx.y * cstride + (size_t)c * C.csz + sidx(C, ic, jc, kc)] = 0.5f * acc;
+}
+
+struct LerpF {
+  int a0, a1;
+  float t;
+};
+// fine coordinate i/2 on the coarse axis of c nodes, low node kept one below
+// the top (multigrid3d.py:465-481)
+__device__ __forceinline__ LerpF pa(int i, int c) {
+  float xf = 0.5f * (float)i;
+  if (xf > (float)(c - 1)) xf = (float)(c - 1);
+  int x0 = (int)xf;
+  if (x0 > c - 2) x0 = c > 1 ? c - 2 : 0;
+  LerpF l;
+  l.a0 = x0;
+  l.a1 = c > 1 ? x0 + 1 : x0;
+  l.t = xf - (float)x0;
+  return l;
+}
+
+__device__ __forceinline__ float cget(const float* eb, const SGeo& C, int i, int j, int k) {
+  return eb[(size_t)scol(i, j, k) * C.csz + sidx(C, i, j, k)];
+}
+
+// e_fine += trilinear(e_coarse) at free fine nodes.
+__global__ void __launch_bounds__(kT)
+k_prolong_add(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
+              const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
+              size_t fstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= F.n) return;
+  const uint32_t ij = fdivu(t, F.dnz);
+  const int k = (int)(t - ij * F.dnz.d);
+  const int i = (int)fdivu(ij, F.dny);
+  const int j = (int)(ij - (uint32_t)i * F.dny.d);
+  const int c = scol(i, j, k);
+  const uint32_t s = sidx(F, i, j, k);
+  if (maskf[(size_t)c * F.csz + s]) return;
+  const float* eb = ec + blockIdx.y * cstride;
+  const LerpF x = pa(i, C.nx), y = pa(j, C.ny), z = pa(k, C.nz);
+  const float c00 = cget(eb, C, x.a0, y.a0, z.a0) * (1.f - x.t) + cget(eb, C, x.a1, y.a0, z.a0) * x.t;
+  const float c10 = cget(eb, C, x.a0, y.a1, z.a0) * (1.f - x.t) + cget(eb, C, x.a1, y.a1, z.a0) * x.t;
+  const float c01 = cget(eb, C, x.a0, y.a0, z.a1) * (1.f - x.t) + cget(eb, C, x.a1, y.a0, z.a1) * x.t;
+  const float c11 = cget(eb, C, x.a0, y.a1, z.a1) * (1.f - x.t) + cget(eb, C, x.a1, y.a1, z.a1) * x.t;
+  const float c0 = c00 * (1.f - y.t) + c10 * y.t;
+  const float c1 = c01 * (1.f - y.t) + c11 * y.t;
+  ef[fstride * blockIdx.y + (size_t)c * F.csz + s] += c0 * (1.f - z.t) + c1 * z.t;
+}
+
+// Coarsest level: red-black SOR in shared memory, one CTA per problem, a
+// fixed number of pairs (the level has at most kBottomMax nodes).
+__global__ void __launch_bounds__(kBottomThreads)
+k_bottom(float* __restrict__ e, const float* __restrict__ g,
+         const uint8_t* __restrict__ mask, SGeo G, float omega, int pairs,
+         size_t pstride) {
+  __shared__ float se[kBottomMax];
+  __shared__ float sg[kBottomMax];
+  __shared__ uint8_t sm[kBottomMax];
+  float* eb = e + blockIdx.x * pstride;
+  const float* gb = g + blockIdx.x * pstride;
+  for (uint32_t t = threadIdx.x; t < G.n; t += blockDim.x) {
+    const int k = (int)(t % G.nz);
+    const int j = (int)((t / G.nz) % G.ny);
+    const int i = (int)(t / ((uint32_t)G.nz * G.ny));
+    const int c = scol(i, j, k);
+    const uint32_t s = sidx(G, i, j, k);
+    se[t] = 0.f;
+    sg[t] = gb[(size_t)c * G.csz + s];
+    sm[t] = mask[(size_t)c * G.csz + s];
+  }
+  __syncthreads();
+  for (int it = 0; it < pairs; it++) {
+    for (int c = 0; c < 2; c++) {
+      for (uint32_t t = threadIdx.x; t < G.n; t += blockDim.x) {
+        const int k = (int)(t % G.nz);
+        const int j = (int)((t / G.nz) % G.ny);
+        const int i = (int)(t / ((uint32_t)G.nz * G.ny));
+        if (scol(i, j, k) != c || sm[t]) continue;
+        const float xm = se[((uint32_t)lo_i(i, G.nx) * G.ny + j) * G.nz + k];
+        const float xp = se[((uint32_t)hi_i(i, G.nx) * G.ny + j) * G.nz + k];
+        const float ym = se[((uint32_t)i * G.ny + lo_i(j, G.ny)) * G.nz + k];
+        const float yp = se[((uint32_t)i * G.ny + hi_i(j, G.ny)) * G.nz + k];
+        const float zm = se[((uint32_t)i * G.ny + j) * G.nz + lo_i(k, G.nz)];
+        const float zp = se[((uint32_t)i * G.ny + j) * G.nz + hi_i(k, G.nz)];
+        const float q = ((((xm + xp) + (ym + yp)) + (zm + zp)) - sg[t]) * (1.0f / 6.0f);
+        se[t] += omega * (q - se[t]);
+      }
+      __syncthreads();
+    }
+  }
+  for (uint32_t t = threadIdx.x; t < G.n; t += blockDim.x) {
+    const int k = (int)(t % G.nz);
+    const int j = (int)((t / G.nz) % G.ny);
+    const int i = (int)(t / ((uint32_t)G.nz * G.ny));
+    eb[(size_t)scol(i, j, k) * G.csz + sidx(G, i, j, k)] = se[t];
+  }
+}
+
+// natural u8 mask -> split u8 mask
+__global__ void k_split_mask(const uint8_t* __restrict__ nat, SGeo G, uint8_t* __restrict__ sp) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= G.n) return;
+  const uint32_t ij = fdivu(t, G.dnz);
+  const int k = (int)(t - ij * G.dnz.d);
+  const int i = (int)fdivu(ij, G.dny);
+  const int j = (int)(ij - (uint32_t)i * G.dny.d);
+  sp[(size_t)scol(i, j, k) * G.csz + sidx(G, i, j, k)] = nat[t];
+}
+
+// ---- FP64 refinement kernels (natural phi64, split g32 / e32) -----------
+
+// g32 = -(float) (scale * r64(phi)) at free nodes, 0 at metal; r64 is the
+// reference's fine residual with theta None (kind kPlain: sum - 6 phi; the
+// Shortley-Weller form is half of it and is scaled by 2 through `scale`).
+__global__ void __launch_bounds__(kT)
+k_resid64(const double* __restrict__ phi, const uint8_t* __restrict__ fixed,
+          SGeo G, float* __restrict__ g, double scale, size_t nstride,
+          size_t pstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= G.n) return;
+  const uint32_t ij = fdivu(t, G.dnz);
+  const int k = (int)(t - ij * G.dnz.d);
+  const int i = (int)fdivu(ij, G.dny);
+  const int j = (int)(ij - (uint32_t)i * G.dny.d);
+  float out = 0.f;
+  if (!fixed[t]) {
+    const double* p = phi + blockIdx.y * nstride;
+    const size_t sx = (size_t)G.ny * G.nz, sy = G.nz;
+    const size_t row = (size_t)i * sx + (size_t)j * sy;
+    const double s = ((p[(size_t)lo_i(i, G.nx) * sx + (size_t)j * sy + k] +
+                       p[(size_t)hi_i(i, G.nx) * sx + (size_t)j * sy + k]) +
+                      (p[(size_t)i * sx + (size_t)lo_i(j, G.ny) * sy + k] +
+                       p[(size_t)i * sx + (size_t)hi_i(j, G.ny) * sy + k])) +
+                     (p[row + lo_i(k, G.nz)] + p[row + hi_i(k, G.nz)]);
+    const double r = s - 6.0 * p[t];
+    out = (float)(-scale * r);
+  }
+  g[blockIdx.y * pstride + (size_t)scol(i, j, k) * G.csz + sidx(G, i, j, k)] = out;
+}
+
+// phi64 += e32 at free nodes; the applied change |phi_new - phi_old| is
+// measured in FP64 and its per-problem maximum goes to dmax[b] (the
+// refinement's convergence norm, the analogue of the V-cycle's full-cycle
+// change, multigrid3d.py:702).
+__global__ void __launch_bounds__(kT)
+k_update64(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
+           const float* __restrict__ e, SGeo G, unsigned long long* dmax,
+           size_t nstride, size_t pstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  unsigned long long key = 0;
+  if (t < G.n && !fixed[t]) {
+    const uint32_t ij = fdivu(t, G.dnz);
+    const int k = (int)(t - ij * G.dnz.d);
+    const int i = (int)fdivu(ij, G.dny);
+    const int j = (int)(ij - (uint32_t)i * G.dny.d);
+    const float d = e[blockIdx.y * pstride + (size_t)scol(i, j, k) * G.csz + sidx(G, i, j, k)];
+    double* q = phi + blockIdx.y * nstride + t;
+    const double old = *q;
+    const double nw = old + (double)d;
+    *q = nw;
+    const double ch = nw - old;
+    key = static_cast<unsigned long long>(__double_as_longlong(ch)) & 0x7fffffffffffffffULL;
+    if (key > 0x7ff0000000000000ULL) key = 0x7ff0000000000000ULL;  // NaN: never converged
+  }
+  key = warp_max_u64(key);
+  __shared__ unsigned long long red[kT / 32];
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = key;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    key = threadIdx.x < kT / 32 ? red[threadIdx.x] : 0ull;
+    key = warp_max_u64(key);
+    if (threadIdx.x == 0 && key) atomicMax(dmax + blockIdx.y, key);
+  }
+}
+
+// phi64[b] = Dirichlet values of problem b at metal, 0 elsewhere; for a
+// basis set the value is v_basis on mask b.
+__global__ void k_init_basis(double* __restrict__ phi, const uint8_t* __restrict__ masks,
+                             uint32_t n, double v, size_t nstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= n) return;
+  phi[blockIdx.y * nstride + t] = masks[(size_t)blockIdx.y * n + t] ? v : 0.0;
+}
+
+__global__ void k_init_vals(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
+                            const double* __restrict__ val, uint32_t n, size_t nstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= n) return;
+  phi[blockIdx.y * nstride + t] = fixed[t] ? val[blockIdx.y * nstride + t] : 0.0;
+}
+
+// ---- host side ----------------------------------------------------------
+
+#define MK(x)                                                                \
+  do {                                                                       \
+    cudaError_t e_ = (x);                                                    \
+    if (e_ != cudaSuccess) {                                                 \
+      set_last_error(std::string(#x) + ": " + cudaGetErrorString(e_));       \
+      throw (int)IG_CUDA_ERROR;                                              \
+    }                                                                        \
+  } while (0)
+
+// Stream-ordered device buffer, move-only.
+template <class T>
+struct Buf {
+  T* p = nullptr;
+  cudaStream_t s = nullptr;
+  Buf() = default;
+  Buf(const Buf&) = delete;
+  Buf& operator=(const Buf&) = delete;
+  Buf(Buf&& o) noexcept : p(o.p), s(o.s) { o.p = nullptr; }
+  Buf& operator=(Buf&& o) noexcept {
+    release();
+    p = o.p;
+    s = o.s;
+    o.p = nullptr;
+    return *this;
+  }
+  void alloc(size_t n, cudaStream_t st) {
+    release();
+    s = st;
+    MK(cudaMallocAsync((void**)&p, std::max<size_t>(n * sizeof(T), 256), st));
+  }
+  void release() {
+    if (p) cudaFreeAsync(p, s);
+    p = nullptr;
+  }
+  ~Buf() { release(); }
+};
+
+struct MLevel {
+  Dims d;
+  SGeo G;
+  Buf<uint8_t> nat;    // natural mask (source of the next coarsening)
+  Buf<uint8_t> mask;   // split mask
+  Buf<float> e, g, r;  // split e, g (per problem); natural r (per problem)
+  size_t pstride = 0;  // 2 * csz
+  size_t rstride = 0;  // n
+};
+
+unsigned nblk(uint32_t n) { return (n + kT - 1) / kT; }
+
+double omega_of(const Dims& d) {
+  double num = 0.0, w = 0.0;
+  const long ns[3] = {d.nx, d.ny, d.nz};
+  for (long q : ns)
+    if (q >= 2) { num += std::cos(M_PI / (double)(q + 1)); w += 1.0; }
+  if (w == 0) return 1.0;
+  const double rho = std::min(num / w, 1.0 - 1e-15);
+  return 2.0 / (1.0 + std::sqrt(1.0 - rho * rho));
+}
+
+bool is_bottom(const Dims& d) {
+  return d.n() <= (size_t)kBottomMax || (d.nx <= 2 && d.ny <= 2 && d.nz <= 2);
+}
+
+// Device bytes a session holds (for admission control by HBM footprint).
+size_t session_bytes(Dims fine, int bmax) {
+  size_t b = fine.n() * (1 + 8 * (size_t)bmax + (size_t)bmax);  // mask, phi, masks/values staging
+  Dims d = fine;
+  while (true) {
+    const size_t csz = (size_t)d.nx * d.ny * ((d.nz + 1) / 2);
+    b += d.n() + 2 * csz + 2 * (2 * csz * 4 * (size_t)bmax);
+    if (is_bottom(d)) break;
+    b += d.n() * 4 * (size_t)bmax;
+    d = coarse_of(d);
+  }
+  return b + 8 * (size_t)bmax;
+}
+
+// One geometry resident on the device: the FP32 multigrid hierarchy for up
+// to bmax problems, the FP64 potentials, and one CUDA graph per batch size.
+struct Session {
+  cudaStream_t s = nullptr;
+  Dims d;
+  int bmax = 1;
+  int B = 1;  // problems of the current call
+  std::vector<MLevel> lv;
+  Buf<double> phi;
+  Buf<uint8_t> fixed;   // natural fine mask
+  Buf<uint8_t> stage;   // per-call staging of basis masks
+  Buf<double> vstage;   // per-call staging of Dirichlet values
+  Buf<unsigned long long> dmax;
+  int nu1 = 2, nu2 = 2, vcycles = 2, bottom_pairs = 40;
+  double resid_scale = 1.0;
+  float bottom_omega = 1.f;
+  std::vector<std::pair<int, cudaGraphExec_t>> graphs;
+
+  ~Session() {
+    for (auto& g : graphs) cudaGraphExecDestroy(g.second);
+    lv.clear();
+    phi.release();
+    fixed.release();
+    stage.release();
+    vstage.release();
+    dmax.release();
+    if (s) {
+      cudaStreamSynchronize(s);
+      cudaStreamDestroy(s);
+    }
+  }
+
+  void build(const uint8_t* metal) {
+    const size_t n = d.n();
+    fixed.alloc(n, s);
+    MK(cudaMemcpyAsync(fixed.p, metal, n, cudaMemcpyDefault, s));
+    Dims c = d;
+    while (true) {
+      MLevel L;
+      L.d = c;
+      L.G = sgeo(c);
+      L.nat.alloc(c.n(), s);
+      if (lv.empty())
+        MK(cudaMemcpyAsync(L.nat.p, fixed.p, n, cudaMemcpyDeviceToDevice, s));
+      else
+        launch_coarsen_any(s, lv.back().nat.p, lv.back().d, L.nat.p, c);
+      L.mask.alloc(2 * (size_t)L.G.csz, s);
+      MK(cudaMemsetAsync(L.mask.p, 1, 2 * (size_t)L.G.csz, s));  // unused slots: metal
+      k_split_mask<<<nblk(L.G.n), kT, 0, s>>>(L.nat.p, L.G, L.mask.p);
+      L.pstride = 2 * (size_t)L.G.csz;
+      L.rstride = L.G.n;
+      L.e.alloc(L.pstride * bmax, s);
+      L.g.alloc(L.pstride * bmax, s);
+      MK(cudaMemsetAsync(L.e.p, 0, L.pstride * bmax * 4, s));
+      MK(cudaMemsetAsync(L.g.p, 0, L.pstride * bmax * 4, s));
+      const bool bottom = is_bottom(c);
+      if (!bottom) L.r.alloc(L.rstride * bmax, s);
+      lv.push_back(std::move(L));
+      if (bottom) break;
+      c = coarse_of(c);
+    }
+    bottom_omega = (float)omega_of(lv.back().d);
+    phi.alloc(n * bmax, s);
+    dmax.alloc(bmax, s);
+    MK(cudaGetLastError());
+  }
+
+  void vcycle(size_t l) {
+    MLevel& a = lv[l];
+    const dim3 gs(nblk(a.G.csz), B), gn(nblk(a.G.n), B);
+    if (l + 1 == lv.size()) {
+      k_bottom<<<B, kBottomThreads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, bottom_omega,
+                                            bottom_pairs, a.pstride);
+      return;
+    }
+    for (int q = 0; q < nu1; q++)
+      for (int c = 0; c < 2; c++)
+        k_gs<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, 1.f, a.pstride);
+    k_resid<<<gn, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p, a.pstride, a.rstride);
+    MLevel& b = lv[l + 1];
+    k_restrict<<<dim3(nblk(b.G.n), B), kT, 0, s>>>(a.r.p, a.G, b.g.p, b.G, a.rstride, b.pstride);
+    if (l + 2 < lv.size()) MK(cudaMemsetAsync(b.e.p, 0, b.pstride * B * 4, s));
+    vcycle(l + 1);
+    k_prolong_add<<<gn, kT, 0, s>>>(b.e.p, b.G, a.e.p, a.mask.p, a.G, b.pstride, a.pstride);
+    for (int q = 0; q < nu2; q++)
+      for (int c = 0; c < 2; c++)
+        k_gs<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, 1.f, a.pstride);
+  }
+
+  // one refinement step: FP64 residual, V-cycles on the correction, update
+  void step_enqueue() {
+    MLevel& f = lv[0];
+    const size_t nstride = f.G.n;
+    const dim3 gn(nblk(f.G.n), B);
+    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, nstride, f.pstride);
+    MK(cudaMemsetAsync(f.e.p, 0, f.pstride * B * 4, s));
+    for (int v = 0; v < vcycles; v++) vcycle(0);
+    MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
+    k_update64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.e.p, f.G, dmax.p, nstride, f.pstride);
+  }
+
+  void step() {
+    cudaGraphExec_t exec = nullptr;
+    for (auto& g : graphs)
+      if (g.first == B) exec = g.second;
+    if (!exec) {
+      cudaGraph_t graph;
+      MK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+      step_enqueue();
+      MK(cudaStreamEndCapture(s, &graph));
+      MK(cudaGraphInstantiate(&exec, graph, 0));
+      MK(cudaGraphDestroy(graph));
+      graphs.push_back({B, exec});
+    }
+    MK(cudaGraphLaunch(exec, s));
+  }
+
+  long launches_per_step() const {
+    long per_v = 1;
+    for (size_t l = 0; l + 1 < lv.size(); l++) per_v += 2 * (nu1 + nu2) + 3;
+    return 2 + per_v * vcycles;
+  }
+};
+
+struct MixedResult {
+  int status;
+  int steps;
+  std::vector<double> dmax;
+};
+
+// Refinement steps until every problem's applied change is below acc.
+MixedResult run_mixed(Session& M, double acc, int max_steps) {
+  std::vector<unsigned long long> h(M.B);
+  MixedResult res{IG_NOT_CONVERGED, 0, std::vector<double>(M.B, 0.0)};
+  for (int it = 0; it < max_steps; it++) {
+    M.step();
+    MK(cudaMemcpyAsync(h.data(), M.dmax.p, 8 * M.B, cudaMemcpyDeviceToHost, M.s));
+    MK(cudaStreamSynchronize(M.s));
+    res.steps = it + 1;
+    bool all = true;
+    for (int b = 0; b < M.B; b++) {
+      res.dmax[b] = bits_to_double(h[b]);
+      if (!(res.dmax[b] < acc)) all = false;
+    }
+    if (all) {
+      res.status = IG_OK;
+      break;
+    }
+  }
+  return res;
+}
+
+std::atomic<long> g_mixed_launches{0};
+
+int finish(Session& S, const MixedResult& r, double* phi_out, int* steps_out,
+           double* dmax_out) {
+  g_mixed_launches.fetch_add(S.launches_per_step() * r.steps);
+  MK(cudaMemcpyAsync(phi_out, S.phi.p, S.d.n() * S.B * 8, cudaMemcpyDefault, S.s));
+  MK(cudaStreamSynchronize(S.s));
+  if (steps_out) *steps_out = r.steps;
+  if (dmax_out) std::memcpy(dmax_out, r.dmax.data(), 8 * S.B);
+  if (r.status != IG_OK) set_last_error("mixed-precision refinement reached its step cap");
+  return r.status;
+}
+
+}  // namespace
+
+long mixed_launch_total() { return g_mixed_launches.load(); }
+
+}  // namespace ig
+
+using namespace ig;
+
+extern "C" {
+
+long ig_mixed_bytes(long nx, long ny, long nz, int max_problems) {
+  if (nx < 1 || ny < 1 || nz < 1 || max_problems < 1) return -1;
+  return (long)session_bytes(Dims{nx, ny, nz}, max_problems);
+}
+
+int ig_mixed_open(const uint8_t* metal, long nx, long ny, long nz,
+                  int max_problems, int stencil, int nu1, int nu2, int vcycles,
+                  void** handle) {
+  set_last_error("");
+  if (!handle || !metal) {
+    set_last_error("null argument");
+    return IG_BAD_ARG;
+  }
+  *handle = nullptr;
+  if (nx < 1 || ny < 1 || nz < 1 || max_problems < 1 || max_problems > 65535 ||
+      (double)nx * ny * nz >= 2147483648.0 ||
+      (double)nx * ny * nz * max_problems >= 9.0e18 || (stencil != 0 && stencil != 1)) {
+    set_last_error("invalid shape, problem count or stencil");
+    return IG_BAD_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    set_last_error("no CUDA device is visible");
+    return IG_NO_DEVICE;
+  }
+  Session* S = new Session();
+  try {
+    MK(cudaStreamCreateWithFlags(&S->s, cudaStreamNonBlocking));
+    S->d = Dims{nx, ny, nz};
+    S->bmax = max_problems;
+    S->nu1 = std::max(0, nu1);
+    S->nu2 = std::max(1, nu2);
+    S->vcycles = std::max(1, vcycles);
+    // the Shortley-Weller residual with unit legs is half the ghost_linear
+    // one: scale it so the correction solves the same equation
+    S->resid_scale = stencil == 0 ? 1.0 : 2.0;
+    S->build(metal);
+    MK(cudaStreamSynchronize(S->s));
+  } catch (int code) {
+    delete S;
+    return code;
+  }
+  *handle = S;
+  return IG_OK;
+}
+
+void ig_mixed_close(void* handle) { delete static_cast<Session*>(handle); }
+
+int ig_mixed_solve_bases(void* handle, const uint8_t* masks, int n_bases,
+                         double v_basis, double acc, int max_steps,
+                         double* phi_out, int* steps_out, double* dmax_out) {
+  set_last_error("");
+  Session* S = static_cast<Session*>(handle);
+  if (!S || !masks || !phi_out || n_bases < 1 || n_bases > S->bmax) {
+    set_last_error("null argument or basis count outside 1..max_problems");
+    return IG_BAD_ARG;
+  }
+  try {
+    const size_t n = S->d.n();
+    S->B = n_bases;
+    if (!S->stage.p) S->stage.alloc(n * S->bmax, S->s);
+    MK(cudaMemcpyAsync(S->stage.p, masks, n * n_bases, cudaMemcpyDefault, S->s));
+    k_init_basis<<<dim3(nblk((uint32_t)n), n_bases), kT, 0, S->s>>>(S->phi.p, S->stage.p,
+                                                                   (uint32_t)n, v_basis, n);
+    MK(cudaGetLastError());
+    const MixedResult r = run_mixed(*S, acc, max_steps);
+    return finish(*S, r, phi_out, steps_out, dmax_out);
+  } catch (int code) {
+    return code;
+  }
+}
+
+int ig_mixed_solve_values(void* handle, const double* vals, int n_problems,
+                          double acc, int max_steps, double* phi_out,
+                          int* steps_out, double* dmax_out) {
+  set_last_error("");
+  Session* S = static_cast<Session*>(handle);
+  if (!S || !vals || !phi_out || n_problems < 1 || n_problems > S->bmax) {
+    set_last_error("null argument or problem count outside 1..max_problems");
+    return IG_BAD_ARG;
+  }
+  try {
+    const size_t n = S->d.n();
+    S->B = n_problems;
+    if (!S->vstage.p) S->vstage.alloc(n * S->bmax, S->s);
+    MK(cudaMemcpyAsync(S->vstage.p, vals, n * n_problems * 8, cudaMemcpyDefault, S->s));
+    k_init_vals<<<dim3(nblk((uint32_t)n), n_problems), kT, 0, S->s>>>(S->phi.p, S->fixed.p,
+                                                                     S->vstage.p, (uint32_t)n, n);
+    MK(cudaGetLastError());
+    const MixedResult r = run_mixed(*S, acc, max_steps);
+    return finish(*S, r, phi_out, steps_out, dmax_out);
+  } catch (int code) {
+    return code;
+  }
+}
+
+int ig_mixed_bases(const uint8_t* metal, const uint8_t* masks, int n_bases,
+                   double v_basis, long nx, long ny, long nz, int stencil,
+                   double acc, int max_steps, int nu1, int nu2, int vcycles,
+                   double* phi_out, int* steps_out, double* dmax_out) {
+  void* h = nullptr;
+  int st = ig_mixed_open(metal, nx, ny, nz, n_bases, stencil, nu1, nu2, vcycles, &h);
+  if (st != IG_OK) return st;
+  st = ig_mixed_solve_bases(h, masks, n_bases, v_basis, acc, max_steps, phi_out,
+                            steps_out, dmax_out);
+  ig_mixed_close(h);
+  return st;
+}
+
+}  // extern "C"

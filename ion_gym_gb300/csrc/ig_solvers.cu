@@ -544,6 +544,8 @@ cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 using namespace ig;
 
+void ig::set_last_error(const std::string& m) { t_err = m; }
+
 extern "C" {
 
 const char* ig_last_error(void) { return t_err.c_str(); }

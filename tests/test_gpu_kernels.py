@@ -37,6 +37,9 @@ def test_div6_is_correctly_rounded():
     bits = (bits & np.uint64(0x800FFFFFFFFFFFFF)) | (expo << np.uint64(52))
     x = bits.view(np.float64)
     x = x[np.isfinite(x) & (np.abs(x) < 1e300)]
+    special = np.array([0.0, -0.0, 5e-324, -5e-324, 1e-310, -2.2e-308, 6.0,
+                        -6.0, 3.0, 1e-300, 1e300, 0.5, 1.0 / 3.0])
+    x = np.concatenate([special, special, x])
     # a 1 x 1 x n grid with every node free: the sweep on colour c reads
     # its two z-neighbours; put x/2 on the neighbours so num = 6 * (x/2) *...
     # Instead drive the residual-free identity directly: sweep_rhs with
