@@ -334,17 +334,227 @@ def run_reference(a):
                 "d2h_bytes_per_step": 0}}), flush=True)
 
 
+def _peak():
+    pk = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    return json.load(open(pk)).get("hbm_gbs") if os.path.exists(pk) else None
+
+
+def run_rings(a):
+    """BASELINE config 3: the 8 unit bases of a seeded ring stack
+    (193x193x385) in one batch, mixed precision to 1e-9 of the span, against
+    the FP64 drop-in (the reference's V-cycle basis door at tol = 1e-9 x
+    span, bit-identical to the reference)."""
+    import ctypes
+    import torch
+    from ion_gym_gb300 import _lib
+    from ion_gym_gb300.workloads import ring_stack
+    from ion_gym_gb300.physics.mixed import MixedSession, solve_bases_mixed
+    from ion_gym_gb300.physics import multigrid3d as MG
+    torch.cuda.set_device(0)
+    L = _lib.lib()
+    masks, box = ring_stack(0)
+    masks = dict(masks)
+    rings = sorted(masks)
+    masks[len(rings) + 1] = box          # grounded box: metal, no basis
+    metal = np.zeros(box.shape, bool)
+    for m in masks.values():
+        metal |= m
+    V, ACC = 1e4, 1e-9
+    sess = MixedSession(metal, len(rings))
+    ring_masks = [masks[i] for i in rings]
+    for _ in range(a.warmup):
+        phi = sess.solve_bases(ring_masks, V, ACC)
+    clocks = Clocks(0)
+    launches0 = L.ig_launch_count()
+    torch.cuda.synchronize()
+    clocks.start()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        phi = sess.solve_bases(ring_masks, V, ACC)
+    el = time.perf_counter() - t0
+    ck = clocks.stop()
+    steps_per_solve = sess.last_steps
+    ms = ctypes.c_double(0)
+    by = ctypes.c_double(0)
+    L.ig_mixed_time_gs(sess._h, len(rings), 20, ctypes.byref(ms),
+                       ctypes.byref(by))
+    achieved = by.value / (ms.value * 1e-3) / 1e9
+    # e2e through the public API (host masks in, host bases out)
+    t1 = time.perf_counter()
+    for _ in range(a.steps):
+        solve_bases_mixed(masks, V, ACC, only=set(rings))
+    el_e2e = time.perf_counter() - t1
+    # the FP64 drop-in on the same bases
+    tf = time.perf_counter()
+    fp = MG.solve_bases_mg(masks, v_basis=V, tol=ACC * V, only=set(rings))
+    el_fp = time.perf_counter() - tf
+    err = max(float(np.abs(phi[b] - fp[i]).max()) / V
+              for b, i in enumerate(rings))
+    n = metal.size
+    peak = _peak()
+    line = {
+        "metric": METRIC, "value": len(rings) * a.steps / el,
+        "unit": "solves/s", "n_gpus": 1, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 sweeps + f64 refinement",
+        "data": "synthetic (seeded ring stack)",
+        "config": {"workload": "ring_stack_193x193x385_8_bases_mixed",
+                   "grid": list(box.shape), "bases": len(rings),
+                   "accuracy_of_span": ACC, "refinement_steps": steps_per_solve,
+                   "l2": "inputs larger than L2"},
+        "fp64_dropin": {"value": len(rings) / el_fp, "unit": "solves/s",
+                        "method": "reference V-cycle basis door, tol 1e-5 V"},
+        "mixed_over_fp64": (len(rings) * a.steps / el) / (len(rings) / el_fp),
+        "max_abs_diff_vs_fp64_of_span": err,
+        "e2e": {"value": len(rings) * a.steps / el_e2e, "unit": "solves/s",
+                "h2d_bytes_per_step": n * (len(masks) + 1),
+                "d2h_bytes_per_step": n * 8 * len(rings)},
+        "gpu_launches": int(L.ig_launch_count() - launches0),
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s",
+                     "frac": achieved / peak if peak else None,
+                     "traffic": None,
+                     "kernel": "k_gs (FP32 red-black split Gauss-Seidel)",
+                     "avg_launch_us": 1e3 * ms.value},
+        "clocks": ck,
+    }
+    if not a.no_cpu:
+        from oracle import port
+        t = time.perf_counter()
+        port.solve_bases_mg(masks, v_basis=V, tol=ACC * V, only={rings[0]})
+        tc = time.perf_counter() - t
+        line["cpu_baseline"] = {
+            "value": 1.0 / tc, "unit": "solves/s", "cores": port.num_threads(),
+            "kind": "port",
+            "sample": f"one basis (ring {rings[0]}) by the reference V-cycle "
+                      f"basis door restated in oracle/ (C kernels, all host "
+                      f"threads), {tc:.1f} s"}
+    sess.close()
+    print(json.dumps(line), flush=True)
+
+
+def run_uneven(a):
+    """BASELINE config 4: 64 seeded geometries, cubic sides from
+    {33,65,97,129,193,257}, 2-16 random electrodes at U(-100,100) V, each
+    solved to 1e-9 of its span by the mixed path; the geometries run
+    concurrently (one resident session and CUDA stream each, `workers`
+    at a time)."""
+    import concurrent.futures as cf
+    import torch
+    from ion_gym_gb300.workloads import random_deck
+    from ion_gym_gb300.physics.mixed import MixedSession
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(2026)
+    sides = rng.choice([33, 65, 97, 129, 193, 257], 64)
+    nel = rng.integers(2, 17, 64)
+    decks = [random_deck(1000 + i, int(s), int(k))
+             for i, (s, k) in enumerate(zip(sides, nel))]
+
+    def solve(d):
+        fixed, val = d
+        with MixedSession(fixed, 1) as s:
+            return s.solve_values(val, 1e-9)
+
+    workers = 8
+    with cf.ThreadPoolExecutor(workers) as ex:
+        list(ex.map(solve, decks[:workers]))              # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        list(ex.map(solve, decks))
+        el = time.perf_counter() - t0
+    nodes = sum(int(s) ** 3 for s in sides)
+    print(json.dumps({
+        "metric": METRIC, "value": 64 / el, "unit": "solves/s", "n_gpus": 1,
+        "steps": 1, "warmup": 1, "ms_per_step": 1e3 * el,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 sweeps + f64 refinement",
+        "data": "synthetic (64 seeded random decks)",
+        "config": {"workload": "uneven_batch_64_mixed", "sides":
+                   [int(s) for s in sides], "nodes": nodes,
+                   "accuracy_of_span": 1e-9, "concurrent_sessions": workers}}),
+        flush=True)
+
+
+def run_serve(a):
+    """BASELINE config 5: Poisson arrivals of basis-solve requests (planar
+    boards up to 512x128x96 with 8-32 extruded electrodes on two layers,
+    plus the grounded box), continuous batching, resident geometries, HBM
+    admission; p50/p99 latency beside throughput."""
+    import torch
+    from ion_gym_gb300.workloads import planar_board
+    from ion_gym_gb300.serve import FieldServer, poisson_schedule, percentile
+    torch.cuda.set_device(0)
+    rng = np.random.default_rng(5)
+    shapes = [(512, 128, 96), (384, 96, 64), (256, 128, 64), (256, 64, 48)]
+    pool = []
+    for i in range(8):
+        shp = shapes[i % len(shapes)]
+        masks, box = planar_board(100 + i, shape=shp,
+                                  n_electrodes=int(rng.integers(8, 33)))
+        masks = {k: m for k, m in masks.items() if m.any()}
+        masks[max(masks) + 1] = box
+        pool.append(masks)
+    srv = FieldServer(workers=a.workers)
+    for d in pool:                                   # warm: resident sessions
+        srv.submit(d).result()
+    srv.completed.clear()
+    arrivals = poisson_schedule(a.rate, a.duration, seed=9)
+    futs = []
+    chosen = []
+    t0 = time.perf_counter()
+    for t in arrivals:
+        dt = t0 + t - time.perf_counter()
+        if dt > 0:
+            time.sleep(dt)
+        k = int(rng.integers(len(pool)))
+        chosen.append(k)
+        futs.append(srv.submit(pool[k]))
+    for f in futs:
+        f.result()
+    el = time.perf_counter() - t0
+    lat = srv.latencies()
+    srv.close()
+    total = [x[2] for x in lat]
+    bases = sum(len(pool[k]) for k in chosen)
+    print(json.dumps({
+        "metric": METRIC, "value": len(lat) / el, "unit": "requests/s",
+        "n_gpus": 1, "steps": len(lat), "warmup": len(pool),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 sweeps + f64 refinement", "data": "synthetic boards",
+        "config": {"workload": "serve_poisson_planar_boards",
+                   "rate_req_s": a.rate, "duration_s": a.duration,
+                   "workers": a.workers, "shapes": shapes},
+        "latency_ms": {"p50": 1e3 * percentile(total, 50),
+                       "p99": 1e3 * percentile(total, 99),
+                       "queue_p50": 1e3 * percentile([x[0] for x in lat], 50),
+                       "service_p50": 1e3 * percentile([x[1] for x in lat],
+                                                       50)},
+        "basis_solves_s": bases / el}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="quad257",
+                    choices=["quad257", "rings", "uneven", "serve"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--rate", type=float, default=20.0)
+    ap.add_argument("--duration", type=float, default=20.0)
+    ap.add_argument("--workers", type=int, default=4)
     a = ap.parse_args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload == "rings":
+        run_rings(a)
+    elif a.workload == "uneven":
+        run_uneven(a)
+    elif a.workload == "serve":
+        run_serve(a)
     else:
         run_ours(a)
 

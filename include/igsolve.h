@@ -160,6 +160,13 @@ long ig_mixed_bytes(long nx, long ny, long nz, int max_problems);
 int ig_mixed_open(const uint8_t *metal, long nx, long ny, long nz,
                   int max_problems, int stencil, int nu1, int nu2, int vcycles,
                   void **handle);
+/* ig_mixed_open with the cycle shape: gamma 1 = V-cycle, 2 = W-cycle (the
+ * coarse levels are cycled twice per visit); smooth_omega: the relaxation
+ * factor of the red-black smoother (1 = Gauss-Seidel). */
+int ig_mixed_open_ex(const uint8_t *metal, long nx, long ny, long nz,
+                     int max_problems, int stencil, int nu1, int nu2,
+                     int vcycles, int gamma, double smooth_omega,
+                     void **handle);
 int ig_mixed_solve_bases(void *handle, const uint8_t *masks, int n_bases,
                          double v_basis, double acc, int max_steps,
                          double *phi_out, int *steps_out, double *dmax_out);
@@ -167,6 +174,12 @@ int ig_mixed_solve_values(void *handle, const double *vals, int n_problems,
                           double acc, int max_steps, double *phi_out,
                           int *steps_out, double *dmax_out);
 void ig_mixed_close(void *handle);
+/* Times `pairs` red-black pairs of the session's fine-level FP32
+ * Gauss-Seidel kernel for n_problems problems with CUDA events on the
+ * session's stream: the average launch (one colour) and its algorithmic
+ * bytes (6.5 B per node and problem). */
+int ig_mixed_time_gs(void *handle, int n_problems, int pairs,
+                     double *ms_per_launch, double *bytes_per_launch);
 
 /* ---- single kernels on device arrays ----------------------------------- */
 

@@ -463,6 +463,8 @@ struct Session {
   Buf<double> vstage;   // per-call staging of Dirichlet values
   Buf<unsigned long long> dmax;
   int nu1 = 2, nu2 = 2, vcycles = 2, bottom_pairs = 40;
+  int gamma = 1;             // 1: V-cycle, 2: W-cycle (coarse levels twice)
+  float smooth_omega = 1.f;  // red-black relaxation factor of the smoother
   double resid_scale = 1.0;
   float bottom_omega = 1.f;
   std::vector<std::pair<int, cudaGraphExec_t>> graphs;
@@ -526,16 +528,20 @@ struct Session {
     }
     for (int q = 0; q < nu1; q++)
       for (int c = 0; c < 2; c++)
-        k_gs<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, 1.f, a.pstride);
+        k_gs<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, smooth_omega, a.pstride);
     k_resid<<<gn, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p, a.pstride, a.rstride);
     MLevel& b = lv[l + 1];
     k_restrict<<<dim3(nblk(b.G.n), B), kT, 0, s>>>(a.r.p, a.G, b.g.p, b.G, a.rstride, b.pstride);
     if (l + 2 < lv.size()) MK(cudaMemsetAsync(b.e.p, 0, b.pstride * B * 4, s));
-    vcycle(l + 1);
+    // the coarse correction: gamma cycles on the coarse equation (the
+    // bottom is solved directly, so once is enough there)
+    const int reps = (l + 2 < lv.size()) ? gamma : 1;
+    for (int q = 0; q < reps; q++) vcycle(l + 1);
     k_prolong_add<<<gn, kT, 0, s>>>(b.e.p, b.G, a.e.p, a.mask.p, a.G, b.pstride, a.pstride);
+    // post-smoothing in the reverse colour order keeps the cycle symmetric
     for (int q = 0; q < nu2; q++)
-      for (int c = 0; c < 2; c++)
-        k_gs<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, 1.f, a.pstride);
+      for (int c = 1; c >= 0; c--)
+        k_gs<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, smooth_omega, a.pstride);
   }
 
   // one refinement step: FP64 residual, V-cycles on the correction, update
@@ -567,9 +573,13 @@ struct Session {
   }
 
   long launches_per_step() const {
-    long per_v = 1;
-    for (size_t l = 0; l + 1 < lv.size(); l++) per_v += 2 * (nu1 + nu2) + 3;
-    return 2 + per_v * vcycles;
+    // launches of one cycle at level l, recursively
+    std::vector<long> c(lv.size(), 1);
+    for (int l = (int)lv.size() - 2; l >= 0; l--) {
+      const int reps = (l + 2 < (int)lv.size()) ? gamma : 1;
+      c[l] = 2 * (nu1 + nu2) + 3 + reps * c[l + 1];
+    }
+    return 2 + c[0] * vcycles;
   }
 };
 
@@ -579,9 +589,14 @@ struct MixedResult {
   std::vector<double> dmax;
 };
 
-// Refinement steps until every problem's applied change is below acc.
+// Refinement steps until every problem is within acc of its converged
+// potential.  The step contraction rho is estimated from successive applied
+// changes d_k / d_{k-1}; the remaining error after step k is then at most
+// about d_k * rho / (1 - rho) (a geometric tail).  A problem is done when
+// that bound and d_k itself are below acc.
 MixedResult run_mixed(Session& M, double acc, int max_steps) {
   std::vector<unsigned long long> h(M.B);
+  std::vector<double> prev(M.B, INFINITY);
   MixedResult res{IG_NOT_CONVERGED, 0, std::vector<double>(M.B, 0.0)};
   for (int it = 0; it < max_steps; it++) {
     M.step();
@@ -590,8 +605,13 @@ MixedResult run_mixed(Session& M, double acc, int max_steps) {
     res.steps = it + 1;
     bool all = true;
     for (int b = 0; b < M.B; b++) {
-      res.dmax[b] = bits_to_double(h[b]);
-      if (!(res.dmax[b] < acc)) all = false;
+      const double d = bits_to_double(h[b]);
+      res.dmax[b] = d;
+      double rho = std::isfinite(prev[b]) && prev[b] > 0 ? d / prev[b] : 1.0;
+      rho = std::min(std::max(rho, 0.05), 0.95);
+      const double tail = d * rho / (1.0 - rho);
+      if (!(d < acc && tail < acc) && !(d == 0.0)) all = false;
+      prev[b] = d;
     }
     if (all) {
       res.status = IG_OK;
@@ -632,6 +652,14 @@ long ig_mixed_bytes(long nx, long ny, long nz, int max_problems) {
 int ig_mixed_open(const uint8_t* metal, long nx, long ny, long nz,
                   int max_problems, int stencil, int nu1, int nu2, int vcycles,
                   void** handle) {
+  return ig_mixed_open_ex(metal, nx, ny, nz, max_problems, stencil, nu1, nu2,
+                          vcycles, 1, 1.0, handle);
+}
+
+int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
+                     int max_problems, int stencil, int nu1, int nu2,
+                     int vcycles, int gamma, double smooth_omega,
+                     void** handle) {
   set_last_error("");
   if (!handle || !metal) {
     set_last_error("null argument");
@@ -658,6 +686,8 @@ int ig_mixed_open(const uint8_t* metal, long nx, long ny, long nz,
     S->nu1 = std::max(0, nu1);
     S->nu2 = std::max(1, nu2);
     S->vcycles = std::max(1, vcycles);
+    S->gamma = std::min(2, std::max(1, gamma));
+    S->smooth_omega = (float)std::min(1.9, std::max(0.5, smooth_omega));
     // the Shortley-Weller residual with unit legs is half the ghost_linear
     // one: scale it so the correction solves the same equation
     S->resid_scale = stencil == 0 ? 1.0 : 2.0;
@@ -672,6 +702,44 @@ int ig_mixed_open(const uint8_t* metal, long nx, long ny, long nz,
 }
 
 void ig_mixed_close(void* handle) { delete static_cast<Session*>(handle); }
+
+int ig_mixed_time_gs(void* handle, int n_problems, int pairs, double* ms_per_launch,
+                     double* bytes_per_launch) {
+  set_last_error("");
+  Session* S = static_cast<Session*>(handle);
+  if (!S || n_problems < 1 || n_problems > S->bmax || pairs < 1) {
+    set_last_error("bad session, problem count or pair count");
+    return IG_BAD_ARG;
+  }
+  try {
+    MLevel& f = S->lv[0];
+    const dim3 gs(nblk(f.G.csz), n_problems);
+    cudaEvent_t e0, e1;
+    MK(cudaEventCreate(&e0));
+    MK(cudaEventCreate(&e1));
+    for (int c = 0; c < 2; c++)  // warm
+      k_gs<<<gs, kT, 0, S->s>>>(f.e.p, f.g.p, f.mask.p, f.G, c, 1.f, f.pstride);
+    MK(cudaEventRecord(e0, S->s));
+    for (int q = 0; q < pairs; q++)
+      for (int c = 0; c < 2; c++)
+        k_gs<<<gs, kT, 0, S->s>>>(f.e.p, f.g.p, f.mask.p, f.G, c, 1.f, f.pstride);
+    MK(cudaEventRecord(e1, S->s));
+    MK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    MK(cudaEventElapsedTime(&ms, e0, e1));
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    g_mixed_launches.fetch_add(2L * pairs + 2);
+    if (ms_per_launch) *ms_per_launch = ms / (2.0 * pairs);
+    // algorithmic bytes of one colour launch: per updated node read its
+    // right-hand side (4) and mask (1), write e (4); per node of the other
+    // colour read e once (4)
+    if (bytes_per_launch) *bytes_per_launch = (double)n_problems * (double)S->d.n() * 6.5;
+    return (int)IG_OK;
+  } catch (int code) {
+    return code;
+  }
+}
 
 int ig_mixed_solve_bases(void* handle, const uint8_t* masks, int n_bases,
                          double v_basis, double acc, int max_steps,

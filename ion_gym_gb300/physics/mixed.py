@@ -21,41 +21,118 @@ from ion_gym_gb300.physics.solver3d import (SolveNotConverged, stencil_code,
                                             _union)
 
 
+# Cycle shape of the FP32 correction solve: nu1/nu2 red-black smoothing
+# pairs before/after the coarse correction, `vcycles` cycles per FP64
+# refinement step, gamma 1 (V) or 2 (W), smoother relaxation factor.
+CYCLE = {"nu1": 2, "nu2": 2, "vcycles": 2, "gamma": 1, "smooth_omega": 1.0}
+
+
+def session_bytes(shape, max_problems):
+    """Device bytes a MixedSession of this grid and batch holds."""
+    return int(_lib.lib().ig_mixed_bytes(*[int(s) for s in shape],
+                                         int(max_problems)))
+
+
+class MixedSession:
+    """One geometry resident on the GPU: its multigrid hierarchy, the FP64
+    potentials of up to `max_problems` problems and the captured CUDA graphs
+    stay allocated between solves.  Each session owns a CUDA stream, so
+    sessions of different geometries, driven from different host threads,
+    run concurrently on the device."""
+
+    def __init__(self, metal, max_problems, stencil="ghost_linear",
+                 nu1=CYCLE["nu1"], nu2=CYCLE["nu2"],
+                 vcycles=CYCLE["vcycles"], gamma=CYCLE["gamma"],
+                 smooth_omega=CYCLE["smooth_omega"]):
+        metal = np.asarray(metal, bool)
+        self.shape = metal.shape
+        self.max_problems = int(max_problems)
+        self.nbytes = session_bytes(self.shape, self.max_problems)
+        self._h = ctypes.c_void_p(None)
+        st = _lib.lib().ig_mixed_open_ex(
+            ptr(as_mask(metal)), *self.shape, self.max_problems,
+            stencil_code(stencil), int(nu1), int(nu2), int(vcycles),
+            int(gamma), float(smooth_omega), ctypes.byref(self._h))
+        _lib.check(st, "MixedSession")
+
+    def _outcome(self, st, steps, dmax, accuracy, span):
+        _lib.check(st, "MixedSession")
+        if st == _lib.IG_NOT_CONVERGED:
+            raise SolveNotConverged(
+                f"mixed-precision refinement: {steps} steps without reaching "
+                f"{accuracy:.1e} of the span {span:g} V (worst applied change "
+                f"{dmax.max():.3e} V)")
+
+    def solve_bases(self, masks, v_basis=1e4, accuracy=1e-9, max_steps=40):
+        """masks: sequence of (nx,ny,nz) bool -> array (B, nx, ny, nz)."""
+        B = len(masks)
+        stack = np.empty((B,) + self.shape, np.uint8)
+        for b, m in enumerate(masks):
+            stack[b] = np.asarray(m, bool)
+        phi = np.empty((B,) + self.shape)
+        steps = ctypes.c_int(0)
+        dmax = np.zeros(B)
+        span = abs(float(v_basis))
+        st = _lib.lib().ig_mixed_solve_bases(
+            self._h, ptr(stack), B, float(v_basis), float(accuracy) * span,
+            int(max_steps), ptr(phi), ctypes.byref(steps), ptr(dmax))
+        self._outcome(st, steps.value, dmax, accuracy, span)
+        self.last_steps = int(steps.value)
+        return phi
+
+    def solve_values(self, vals, accuracy=1e-9, max_steps=40):
+        """vals: (P, nx, ny, nz) Dirichlet values (read at the metal nodes)
+        -> array (P, nx, ny, nz); accuracy is relative to each problem's
+        span of Dirichlet values (at least 1 V)."""
+        vals = np.ascontiguousarray(vals, np.float64)
+        if vals.ndim == 3:
+            vals = vals[None]
+        P = vals.shape[0]
+        phi = np.empty_like(vals)
+        steps = ctypes.c_int(0)
+        dmax = np.zeros(P)
+        span = max(float(np.ptp(vals)), 1.0)
+        st = _lib.lib().ig_mixed_solve_values(
+            self._h, ptr(vals), P, float(accuracy) * span, int(max_steps),
+            ptr(phi), ctypes.byref(steps), ptr(dmax))
+        self._outcome(st, steps.value, dmax, accuracy, span)
+        self.last_steps = int(steps.value)
+        return phi
+
+    def close(self):
+        if self._h:
+            _lib.lib().ig_mixed_close(self._h)
+            self._h = ctypes.c_void_p(None)
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def solve_bases_mixed(masks, v_basis=1e4, accuracy=1e-9,
-                      stencil="ghost_linear", only=None, nu1=2, nu2=2,
-                      vcycles=2, max_steps=40, return_stats=False):
+                      stencil="ghost_linear", only=None, max_steps=40,
+                      return_stats=False, **cycle):
     """All bases in one batch.  Returns {index: phi}; with return_stats also
-    {"steps": refinement steps, "dmax": {index: last applied change}}."""
-    code = stencil_code(stencil)
+    {"steps": refinement steps}.  cycle: overrides of CYCLE."""
     metal = _union(masks)
     items = [(i, np.asarray(m, bool)) for i, m in sorted(masks.items())
              if only is None or i in only]
     if not items:
-        return ({}, {"steps": 0, "dmax": {}}) if return_stats else {}
-    shape = metal.shape
-    n = metal.size
-    B = len(items)
-    stack = np.empty((B,) + shape, np.uint8)
-    for b, (_, m) in enumerate(items):
-        stack[b] = m
-    phi = np.empty((B,) + shape)
-    steps = ctypes.c_int(0)
-    dmax = np.zeros(B)
-    acc = float(accuracy) * abs(float(v_basis))
-    L = _lib.lib()
-    st = L.ig_mixed_bases(ptr(as_mask(metal)), ptr(stack), B, float(v_basis),
-                          *shape, code, acc, int(max_steps), int(nu1),
-                          int(nu2), int(vcycles), ptr(phi),
-                          ctypes.byref(steps), ptr(dmax))
-    _lib.check(st, "solve_bases_mixed")
-    if st == _lib.IG_NOT_CONVERGED:
-        raise SolveNotConverged(
-            f"mixed-precision refinement: {steps.value} steps without every "
-            f"basis reaching {accuracy:.1e} of the span (worst applied change "
-            f"{dmax.max():.3e} V)")
+        return ({}, {"steps": 0}) if return_stats else {}
+    with MixedSession(metal, len(items), stencil=stencil,
+                      **{**CYCLE, **cycle}) as s:
+        phi = s.solve_bases([m for _, m in items], v_basis, accuracy,
+                            max_steps)
+        steps = s.last_steps
     out = {i: phi[b] for b, (i, _) in enumerate(items)}
     if return_stats:
-        return out, {"steps": int(steps.value),
-                     "dmax": {i: float(dmax[b]) for b, (i, _) in
-                              enumerate(items)}}
+        return out, {"steps": steps}
     return out

@@ -1,0 +1,208 @@
+"""A request loop for basis solves with continuous batching.
+
+Requests (a deck: {electrode index: mask}, solved into unit bases at
+v_basis) arrive at any time.  Each admitted request runs on a worker thread
+that drives its own resident MixedSession (own CUDA stream), so requests
+that arrive while others are on the GPU start as soon as a worker slot and
+device memory free up, and their kernels overlap on the device.
+
+Admission is by HBM footprint: a request needs ig_mixed_bytes(grid, bases)
+of device memory; it waits until the sum of the footprints of the sessions
+in use fits the budget.  Finished geometries stay resident (keyed by the
+bytes of their metal mask and basis count) and are reused by a later request
+for the same geometry -- an edited deck whose metal changed gets a new
+session; least-recently-used idle sessions are closed when the budget is
+needed.
+
+Each result is computed by the same kernels in the same order whether the
+request runs alone or among others (sessions share no memory), so it is the
+same alone and in the mix (tests/test_gpu_serve.py).
+"""
+import hashlib
+import threading
+import time
+from collections import OrderedDict
+from concurrent.futures import Future
+
+import numpy as np
+
+from ion_gym_gb300.physics.mixed import MixedSession, session_bytes
+
+
+class Request:
+    __slots__ = ("rid", "masks", "v_basis", "accuracy", "arrival", "start",
+                 "end", "future", "key", "bytes", "n_bases", "shape")
+
+    def __init__(self, rid, masks, v_basis, accuracy, bytes_fn):
+        self.rid = rid
+        self.masks = masks
+        self.v_basis = v_basis
+        self.accuracy = accuracy
+        self.arrival = time.perf_counter()
+        self.start = self.end = None
+        self.future = Future()
+        first = np.asarray(next(iter(masks.values())), bool)
+        self.shape = first.shape
+        self.n_bases = len(masks)
+        metal = np.zeros(self.shape, bool)
+        for m in masks.values():
+            metal |= np.asarray(m, bool)
+        h = hashlib.sha256(np.packbits(metal).tobytes())
+        h.update(repr((self.shape, self.n_bases)).encode())
+        self.key = h.hexdigest()
+        self.bytes = bytes_fn(self.shape, self.n_bases)
+
+
+class FieldServer:
+    """Continuous-batching basis-solve server on one GPU.
+
+    workers: requests in flight at once (CUDA streams in use).
+    hbm_budget: device bytes the resident sessions may hold (default: 80 %
+    of the free memory at start-up).
+    session_factory / bytes_fn: the session class and its footprint
+    function (MixedSession and session_bytes; replaceable for tests of the
+    admission logic without a GPU)."""
+
+    def __init__(self, workers=4, hbm_budget=None, device=0,
+                 session_factory=MixedSession, bytes_fn=session_bytes):
+        self.device = device
+        self._factory = session_factory
+        self._bytes_fn = bytes_fn
+        if device is not None:
+            import torch
+            torch.cuda.set_device(device)
+        if hbm_budget is None:
+            import torch
+            free, _ = torch.cuda.mem_get_info(device)
+            hbm_budget = int(0.8 * free)
+        self.budget = int(hbm_budget)
+        self._cv = threading.Condition()
+        self._queue = []
+        self._in_use = 0                  # bytes of sessions running
+        self._idle = OrderedDict()        # key -> session (resident, idle)
+        self._idle_bytes = 0
+        self._closed = False
+        self._next = 0
+        self.completed = []
+        self._threads = [threading.Thread(target=self._worker, daemon=True)
+                         for _ in range(int(workers))]
+        for t in self._threads:
+            t.start()
+
+    # -------------------------------------------------------------- API
+    def submit(self, masks, v_basis=1e4, accuracy=1e-9):
+        """Queue a deck; returns a Future of {index: basis float64}."""
+        with self._cv:
+            if self._closed:
+                raise RuntimeError("server is closed")
+            r = Request(self._next, dict(sorted(masks.items())), v_basis,
+                        accuracy, self._bytes_fn)
+            self._next += 1
+            if r.bytes > self.budget:
+                r.future.set_exception(MemoryError(
+                    f"request needs {r.bytes} device bytes, budget "
+                    f"{self.budget}"))
+                return r.future
+            self._queue.append(r)
+            self._cv.notify_all()
+        return r.future
+
+    def close(self):
+        with self._cv:
+            self._closed = True
+            self._cv.notify_all()
+        for t in self._threads:
+            t.join()
+        for s in self._idle.values():
+            s.close()
+        self._idle.clear()
+
+    def latencies(self):
+        """(queue wait, service, total) seconds of every finished request."""
+        return [(r.start - r.arrival, r.end - r.start, r.end - r.arrival)
+                for r in self.completed]
+
+    # -------------------------------------------------------------- internals
+    def _admit(self):
+        """Pick the oldest queued request that fits; returns (request,
+        session or None).  Caller holds the lock."""
+        for i, r in enumerate(self._queue):
+            sess = self._idle.pop(r.key, None)
+            if sess is not None:
+                self._idle_bytes -= sess.nbytes
+                self._in_use += sess.nbytes
+                del self._queue[i]
+                return r, sess
+            # evict idle sessions (least recently used first) until it fits
+            while (self._in_use + self._idle_bytes + r.bytes > self.budget
+                   and self._idle):
+                _, old = self._idle.popitem(last=False)
+                self._idle_bytes -= old.nbytes
+                old.close()
+            if self._in_use + self._idle_bytes + r.bytes <= self.budget:
+                self._in_use += r.bytes
+                del self._queue[i]
+                return r, None
+            return None, None       # the oldest waits: no overtaking by size
+        return None, None
+
+    def _worker(self):
+        if self.device is not None:
+            import torch
+            torch.cuda.set_device(self.device)
+        while True:
+            with self._cv:
+                while True:
+                    if self._closed and not self._queue:
+                        return
+                    r, sess = self._admit()
+                    if r is not None:
+                        break
+                    self._cv.wait(0.05)
+            r.start = time.perf_counter()
+            held = sess.nbytes if sess is not None else r.bytes
+            try:
+                if sess is None:
+                    metal = np.zeros(r.shape, bool)
+                    for m in r.masks.values():
+                        metal |= np.asarray(m, bool)
+                    sess = self._factory(metal, r.n_bases)
+                phi = sess.solve_bases(list(r.masks.values()), r.v_basis,
+                                       r.accuracy)
+                result = {i: phi[b] for b, i in enumerate(r.masks)}
+                err = None
+            except Exception as e:     # delivered through the future
+                result, err = None, e
+            r.end = time.perf_counter()
+            with self._cv:
+                self._in_use -= held
+                if sess is not None:
+                    if r.key in self._idle:      # an identical deck ran too
+                        sess.close()
+                    else:
+                        self._idle[r.key] = sess
+                        self._idle_bytes += sess.nbytes
+                self.completed.append(r)
+                self._cv.notify_all()
+            if err is None:
+                r.future.set_result(result)
+            else:
+                r.future.set_exception(err)
+
+
+def poisson_schedule(rate, duration, seed=0):
+    """Arrival times of a Poisson process of `rate` per second."""
+    rng = np.random.default_rng(seed)
+    t, out = 0.0, []
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            return out
+        out.append(t)
+
+
+def percentile(values, q):
+    v = np.sort(np.asarray(values))
+    if len(v) == 0:
+        return None
+    return float(np.percentile(v, q))

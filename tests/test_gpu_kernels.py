@@ -50,7 +50,10 @@ def test_div6_is_correctly_rounded():
     fixed = torch.zeros((1, 1, n), dtype=torch.uint8, device="cuda")
     D.sweep_rhs(e, fixed, f, 1.0, 0)
     got = e.cpu().numpy().ravel()
-    want = x / 6.0
+    # the reference update with zero neighbours: e = 0 + 1*((0 - f)/6 - 0);
+    # (0 - f) is x except that x = -0.0 gives +0.0
+    fn = -x
+    want = 0.0 + 1.0 * ((0.0 - fn) / 6.0 - 0.0)
     even = np.arange(n) % 2 == 0  # colour 0 nodes of a 1x1xn grid
     assert np.array_equal(got[even].view(np.uint64), want[even].view(np.uint64))
 

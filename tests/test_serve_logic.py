@@ -1,0 +1,93 @@
+"""Admission, reuse and eviction of the request loop, on the CPU with a fake
+session (no GPU): requests wait while the HBM budget is held, resident
+geometries are reused, idle sessions are evicted least-recently-used first,
+and an oversized request fails at once."""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from ion_gym_gb300.serve import FieldServer, poisson_schedule, percentile
+
+
+class FakeSession:
+    opened = []
+    closed = []
+    lock = threading.Lock()
+    running = 0
+    peak = 0
+    hold = 0.05
+
+    def __init__(self, metal, n):
+        self.nbytes = 100 * n
+        self.shape = metal.shape
+        with FakeSession.lock:
+            FakeSession.opened.append(self)
+
+    def solve_bases(self, masks, v_basis, accuracy):
+        with FakeSession.lock:
+            FakeSession.running += 1
+            FakeSession.peak = max(FakeSession.peak, FakeSession.running)
+        time.sleep(FakeSession.hold)
+        with FakeSession.lock:
+            FakeSession.running -= 1
+        return np.stack([np.where(np.asarray(m), v_basis, 0.0) for m in masks])
+
+    def close(self):
+        FakeSession.closed.append(self)
+
+
+def _deck(seed, n_bases, shape=(6, 5, 4)):
+    rng = np.random.default_rng(seed)
+    return {i + 1: rng.random(shape) < 0.2 for i in range(n_bases)}
+
+
+@pytest.fixture(autouse=True)
+def _reset():
+    FakeSession.opened, FakeSession.closed = [], []
+    FakeSession.running = FakeSession.peak = 0
+    yield
+
+
+def _server(workers, budget):
+    return FieldServer(workers=workers, hbm_budget=budget, device=None,
+                       session_factory=FakeSession,
+                       bytes_fn=lambda shape, n: 100 * n)
+
+
+def test_budget_limits_concurrency():
+    srv = _server(workers=4, budget=450)       # two 2-basis decks fit at once
+    futs = [srv.submit(_deck(s, 2)) for s in range(6)]
+    for f in futs:
+        assert sorted(f.result(timeout=10)) == [1, 2]
+    srv.close()
+    assert FakeSession.peak <= 2
+    assert len(srv.completed) == 6
+
+
+def test_resident_geometry_is_reused_and_lru_evicted():
+    srv = _server(workers=1, budget=400)
+    a, b = _deck(1, 2), _deck(2, 2)
+    srv.submit(a).result(timeout=10)
+    srv.submit(a).result(timeout=10)           # same metal: reuse
+    assert len(FakeSession.opened) == 1
+    srv.submit(b).result(timeout=10)           # fits beside a (400)
+    assert len(FakeSession.opened) == 2 and not FakeSession.closed
+    srv.submit(_deck(3, 3)).result(timeout=10)  # 300: evicts both idle decks
+    assert len(FakeSession.closed) == 2
+    srv.close()
+
+
+def test_oversized_request_fails_fast():
+    srv = _server(workers=1, budget=150)
+    with pytest.raises(MemoryError):
+        srv.submit(_deck(1, 2)).result(timeout=10)
+    srv.close()
+
+
+def test_schedule_and_percentiles():
+    t = poisson_schedule(50.0, 20.0, seed=3)
+    assert 800 < len(t) < 1200 and all(np.diff(t) > 0)
+    assert percentile([1, 2, 3, 4], 50) == 2.5
+    assert percentile([], 99) is None
