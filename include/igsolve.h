@@ -181,6 +181,33 @@ void ig_mixed_close(void *handle);
 int ig_mixed_time_gs(void *handle, int n_problems, int pairs,
                      double *ms_per_launch, double *bytes_per_launch);
 
+/* ig_cascadic_relres for callers that cannot allocate device memory (no
+ * counterpart in the reference).  Some callers may not call cudaMalloc, or
+ * let a library call it for them, while they run: a serving process that
+ * reserved its HBM up front and lends the solver only its own buffers, a
+ * framework custom call that must not allocate outside its allocator, a
+ * latency-bound loop where an allocation could stall on the driver.  This
+ * entry point allocates nothing: fixed, val and phi_out are DEVICE arrays,
+ * the solve iterates in phi_out, and the coarse levels live in one static
+ * device array of IG_NOALLOC_SCRATCH_BYTES that every GPU loading the
+ * library holds until exit.  A grid whose coarse levels (about 2.4 bytes per
+ * fine node) do not fit is refused with IG_BAD_ARG.  All calls share that
+ * array and it keeps the last call's contents: calls that overlap on the GPU
+ * race, so serialise them.  The first call on a device resolves the array's
+ * device address (make it before any stream capture).  stream: the caller's
+ * cudaStream_t (NULL = legacy default stream).  Same results, bit for bit,
+ * as ig_cascadic_relres. */
+#define IG_NOALLOC_SCRATCH_BYTES (48u * 1024u * 1024u)
+int ig_cascadic_relres_noalloc(const uint8_t *fixed, const double *val,
+                               long nx, long ny, long nz, double rel_tol,
+                               long max_sweeps, int min_coarse,
+                               int max_levels, double level_tol_factor,
+                               const double *level_omega, int n_level_omega,
+                               int check_every, double *phi_out,
+                               long *sweeps_out, double *relres_out,
+                               long *total_pairs_out, int *levels_out,
+                               void *stream);
+
 /* ---- single kernels on device arrays ----------------------------------- */
 
 /* solver3d._sweep (solver3d.py:131-198); theta NULL = all ones.  The max

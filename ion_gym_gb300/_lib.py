@@ -75,6 +75,9 @@ SIGNATURES = {
     "ig_mixed_solve_values": (_i, [_p, _p, _i, _d, _i, _p, _pi, _p]),
     "ig_mixed_close": (None, [_p]),
     "ig_mixed_time_gs": (_i, [_p, _i, _i, _pd, _pd]),
+    "ig_cascadic_relres_noalloc": (_i, [_p, _p, _l, _l, _l, _d, _l, _i, _i,
+                                        _d, _p, _i, _i, _p, _pl, _pd, _pl,
+                                        _pi, _p]),
 }
 
 _lib = None
