@@ -160,13 +160,18 @@ long ig_mixed_bytes(long nx, long ny, long nz, int max_problems);
 int ig_mixed_open(const uint8_t *metal, long nx, long ny, long nz,
                   int max_problems, int stencil, int nu1, int nu2, int vcycles,
                   void **handle);
-/* ig_mixed_open with the cycle shape: gamma 1 = V-cycle, 2 = W-cycle (the
- * coarse levels are cycled twice per visit); smooth_omega: the relaxation
- * factor of the red-black smoother (1 = Gauss-Seidel). */
+/* ig_mixed_open with the method and cycle shape.  method 1 (default of
+ * ig_mixed_open): flexible conjugate gradients on the FP32 correction,
+ * preconditioned by one multigrid cycle, cg_iters iterations per FP64
+ * refinement (the correction is then added to the FP64 potential and the
+ * carried residual replaced by the exact FP64 one); method 0: plain defect
+ * correction with `vcycles` cycles per refinement.  gamma 1 = V-cycle,
+ * 2 = W-cycle (coarse levels cycled twice per visit); smooth_omega: the
+ * relaxation factor of the red-black smoother (1 = Gauss-Seidel). */
 int ig_mixed_open_ex(const uint8_t *metal, long nx, long ny, long nz,
                      int max_problems, int stencil, int nu1, int nu2,
-                     int vcycles, int gamma, double smooth_omega,
-                     void **handle);
+                     int vcycles, int gamma, double smooth_omega, int method,
+                     int cg_iters, void **handle);
 int ig_mixed_solve_bases(void *handle, const uint8_t *masks, int n_bases,
                          double v_basis, double acc, int max_steps,
                          double *phi_out, int *steps_out, double *dmax_out);

@@ -51,10 +51,11 @@ __device__ __forceinline__ uint32_t fdivu(uint32_t n, const FastDiv& f) {
 
 // Geometry of one level in split layout.
 struct SGeo {
-  int nx, ny, nz, H;        // H = (nz + 1) / 2 slots per colour row
+  int nx, ny, nz, H;        // H: slots per colour row, (nz + 1) / 2 rounded
+                            // up to a multiple of 4 (16-byte aligned rows)
   uint32_t csz;             // nx * ny * H (one colour array)
   uint32_t n;               // nx * ny * nz (natural)
-  FastDiv dH, dny, dnz;
+  FastDiv dH, dny, dnz, dH4;
 };
 
 SGeo sgeo(const Dims& d) {
@@ -62,10 +63,11 @@ SGeo sgeo(const Dims& d) {
   g.nx = (int)d.nx;
   g.ny = (int)d.ny;
   g.nz = (int)d.nz;
-  g.H = (int)((d.nz + 1) / 2);
+  g.H = (int)((((d.nz + 1) / 2) + 3) & ~3L);
   g.csz = (uint32_t)(d.nx * d.ny * g.H);
   g.n = (uint32_t)d.n();
   g.dH = FastDiv((uint32_t)g.H);
+  g.dH4 = FastDiv((uint32_t)(g.H / 4));
   g.dny = FastDiv((uint32_t)d.ny);
   g.dnz = FastDiv((uint32_t)d.nz);
   return g;
@@ -86,7 +88,8 @@ __device__ __forceinline__ int scol(int i, int j, int k) { return (i + j + k) & 
 __device__ __forceinline__ float nbr_sum(const SGeo& g, const float* __restrict__ own,
                                          const float* __restrict__ oth, int i,
                                          int j, int m, int k, uint32_t self) {
-  const float me = own[self];
+  const bool flat = g.nx == 1 || g.ny == 1 || g.nz == 1;
+  const float me = flat ? own[self] : 0.f;
   const float xm = g.nx > 1 ? oth[((uint32_t)lo_i(i, g.nx) * g.ny + j) * g.H + m] : me;
   const float xp = g.nx > 1 ? oth[((uint32_t)hi_i(i, g.nx) * g.ny + j) * g.H + m] : me;
   const float ym = g.ny > 1 ? oth[((uint32_t)i * g.ny + lo_i(j, g.ny)) * g.H + m] : me;
@@ -102,26 +105,130 @@ __device__ __forceinline__ float nbr_sum(const SGeo& g, const float* __restrict_
 
 // ---- FP32 kernels on split arrays (blockIdx.y = problem) ----------------
 
-// One red-black colour of Gauss-Seidel / SOR on A e = g.
+// Four consecutive slots m0..m0+3 of one colour row per thread, 16-byte
+// loads of the neighbour rows (the split layout makes the x/y neighbours of
+// slot m the slots m of the adjacent rows, and the z neighbours slots m-1+p
+// and m+p of the other colour's own row).  Threads whose slots touch a face
+// in z, or grids with a size-1 axis, take the per-slot path.
+__device__ __forceinline__ float4 ld4(const float* p) {
+  return *reinterpret_cast<const float4*>(p);
+}
+
 __global__ void __launch_bounds__(kT)
-k_gs(float* __restrict__ e, const float* __restrict__ g, const uint8_t* __restrict__ mask,
-     SGeo G, int c, float omega, size_t pstride) {
+k_gs4(float* __restrict__ e, const float* __restrict__ g,
+      const uint8_t* __restrict__ mask, SGeo G, int c, float omega,
+      size_t pstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  const uint32_t nq = G.csz >> 2;
+  if (t >= nq) return;
+  const uint32_t ij = fdivu(t, G.dH4);
+  const int m0 = 4 * (int)(t - ij * G.dH4.d);
+  const int i = (int)fdivu(ij, G.dny);
+  const int j = (int)(ij - (uint32_t)i * G.dny.d);
+  const int p = (i + j + c) & 1;
+  const uint32_t row = ij * (uint32_t)G.H;
+  const uint32_t base = row + m0;
+  const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + (size_t)c * G.csz + base);
+  if (mk.x & mk.y & mk.z & mk.w) return;  // all metal or unused slots
+  float* eb = e + blockIdx.y * pstride;
+  float* own = eb + (size_t)c * G.csz;
+  const float* oth = eb + (size_t)(1 - c) * G.csz;
+  const float4 gg = ld4(g + blockIdx.y * pstride + (size_t)c * G.csz + base);
+  const int kmax = 2 * (m0 + 3) + p;
+  float q[4];
+  const bool fast = G.nx > 1 && G.ny > 1 && G.nz > 1 && m0 >= 1 && kmax <= G.nz - 2;
+  if (fast) {
+    const float4 xm = ld4(oth + ((uint32_t)lo_i(i, G.nx) * G.ny + j) * G.H + m0);
+    const float4 xp = ld4(oth + ((uint32_t)hi_i(i, G.nx) * G.ny + j) * G.H + m0);
+    const float4 ym = ld4(oth + ((uint32_t)i * G.ny + lo_i(j, G.ny)) * G.H + m0);
+    const float4 yp = ld4(oth + ((uint32_t)i * G.ny + hi_i(j, G.ny)) * G.H + m0);
+    const float4 zc = ld4(oth + base);
+    // z neighbours of slot m: slots m-1+p and m+p of the other colour row
+    float z[5];
+    if (p == 0) {
+      z[0] = oth[base - 1]; z[1] = zc.x; z[2] = zc.y; z[3] = zc.z; z[4] = zc.w;
+    } else {
+      z[0] = zc.x; z[1] = zc.y; z[2] = zc.z; z[3] = zc.w; z[4] = oth[base + 4];
+    }
+    q[0] = ((xm.x + xp.x) + (ym.x + yp.x)) + (z[0] + z[1]);
+    q[1] = ((xm.y + xp.y) + (ym.y + yp.y)) + (z[1] + z[2]);
+    q[2] = ((xm.z + xp.z) + (ym.z + yp.z)) + (z[2] + z[3]);
+    q[3] = ((xm.w + xp.w) + (ym.w + yp.w)) + (z[3] + z[4]);
+  } else {
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int k = 2 * (m0 + u) + p;
+      q[u] = k < G.nz ? nbr_sum(G, own, oth, i, j, m0 + u, k, base + u) : 0.f;
+    }
+  }
+  const float gv[4] = {gg.x, gg.y, gg.z, gg.w};
+  const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    if (mv[u]) continue;
+    const float nv = (q[u] - gv[u]) * (1.0f / 6.0f);
+    own[base + u] = omega == 1.0f ? nv : own[base + u] + omega * (nv - own[base + u]);
+  }
+}
+
+// Residual r = g - A e of colour 0 only, in split layout.  After a red-black
+// Gauss-Seidel pair that ended on colour 1 the residual of colour 1 is zero
+// (each colour-1 node was just solved exactly against its neighbours), so
+// colour 0 carries the whole residual.
+__global__ void __launch_bounds__(kT)
+k_resid0(const float* __restrict__ e, const float* __restrict__ g,
+         const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ r,
+         size_t pstride) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= G.csz) return;
   const uint32_t ij = fdivu(t, G.dH);
   const int m = (int)(t - ij * G.dH.d);
   const int i = (int)fdivu(ij, G.dny);
   const int j = (int)(ij - (uint32_t)i * G.dny.d);
-  const int k = 2 * m + ((i + j + c) & 1);
-  if (k >= G.nz) return;
-  if (mask[(size_t)c * G.csz + t]) return;
-  float* eb = e + blockIdx.y * pstride;
-  const float* gb = g + blockIdx.y * pstride;
-  float* own = eb + (size_t)c * G.csz;
-  const float* oth = eb + (size_t)(1 - c) * G.csz;
-  const float s = nbr_sum(G, own, oth, i, j, m, k, t);
-  const float q = (s - gb[(size_t)c * G.csz + t]) * (1.0f / 6.0f);
-  own[t] = omega == 1.0f ? q : own[t] + omega * (q - own[t]);
+  const int k = 2 * m + ((i + j) & 1);
+  float out = 0.f;
+  if (k < G.nz && !mask[t]) {
+    const float* eb = e + blockIdx.y * pstride;
+    const float a = nbr_sum(G, eb, eb + G.csz, i, j, m, k, t) - 6.0f * eb[t];
+    out = g[blockIdx.y * pstride + t] - a;
+  }
+  r[blockIdx.y * (size_t)G.csz + t] = out;
+}
+
+// 4 x full weighting when only colour 0 of the fine residual is nonzero:
+// around a coarse node (fine centre 2c, colour 0) the colour-0 points are
+// the centre (weight 1) and the 12 edge neighbours (weight 1/4); the faces
+// and corners are colour 1.  Clamped edges as in the 27-point form.
+__global__ void __launch_bounds__(kT)
+k_restrict0(const float* __restrict__ r0, SGeo F, float* __restrict__ gc, SGeo C,
+            size_t cstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= C.n) return;
+  const uint32_t ij = fdivu(t, C.dnz);
+  const int kc = (int)(t - ij * C.dnz.d);
+  const int ic = (int)fdivu(ij, C.dny);
+  const int jc = (int)(ij - (uint32_t)ic * C.dny.d);
+  const float* rb = r0 + blockIdx.y * (size_t)F.csz;
+  float acc = 0.f;
+#pragma unroll
+  for (int di = -1; di <= 1; di++) {
+    const int ii = min(max(2 * ic + di, 0), F.nx - 1);
+    const float wi = di == 0 ? 1.f : 0.5f;
+#pragma unroll
+    for (int dj = -1; dj <= 1; dj++) {
+      const int jj = min(max(2 * jc + dj, 0), F.ny - 1);
+      const float wj = dj == 0 ? 1.f : 0.5f;
+#pragma unroll
+      for (int dk = -1; dk <= 1; dk++) {
+        const int kk = min(max(2 * kc + dk, 0), F.nz - 1);
+        if ((ii + jj + kk) & 1) continue;   // colour 1: zero residual
+        const float wk = dk == 0 ? 1.f : 0.5f;
+        acc += wi * wj * wk * rb[sidx(F, ii, jj, kk)];
+      }
+    }
+  }
+  const int c = scol(ic, jc, kc);
+  gc[blockIdx.y * cstride + (size_t)c * C.csz + sidx(C, ic, jc, kc)] = 0.5f * acc;
 }
 
 // r = g - A e on natural layout (0 at metal).
@@ -203,7 +310,9 @@ __device__ __forceinline__ float cget(const float* eb, const SGeo& C, int i, int
   return eb[(size_t)scol(i, j, k) * C.csz + sidx(C, i, j, k)];
 }
 
-// e_fine += trilinear(e_coarse) at free fine nodes.
+// e_fine += trilinear(e_coarse) at free fine nodes.  Each axis weight is 0,
+// 1/2 or 1 (fine node i sits at i/2 in coarse units), so a fine node reads
+// only the 1, 2, 4 or 8 coarse values whose weight is nonzero.
 __global__ void __launch_bounds__(kT)
 k_prolong_add(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
               const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
@@ -219,13 +328,23 @@ k_prolong_add(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
   if (maskf[(size_t)c * F.csz + s]) return;
   const float* eb = ec + blockIdx.y * cstride;
   const LerpF x = pa(i, C.nx), y = pa(j, C.ny), z = pa(k, C.nz);
-  const float c00 = cget(eb, C, x.a0, y.a0, z.a0) * (1.f - x.t) + cget(eb, C, x.a1, y.a0, z.a0) * x.t;
-  const float c10 = cget(eb, C, x.a0, y.a1, z.a0) * (1.f - x.t) + cget(eb, C, x.a1, y.a1, z.a0) * x.t;
-  const float c01 = cget(eb, C, x.a0, y.a0, z.a1) * (1.f - x.t) + cget(eb, C, x.a1, y.a0, z.a1) * x.t;
-  const float c11 = cget(eb, C, x.a0, y.a1, z.a1) * (1.f - x.t) + cget(eb, C, x.a1, y.a1, z.a1) * x.t;
-  const float c0 = c00 * (1.f - y.t) + c10 * y.t;
-  const float c1 = c01 * (1.f - y.t) + c11 * y.t;
-  ef[fstride * blockIdx.y + (size_t)c * F.csz + s] += c0 * (1.f - z.t) + c1 * z.t;
+  int xi[2], yi[2], zi[2];
+  float xw[2], yw[2], zw[2];
+  int nxw = 0, nyw = 0, nzw = 0;
+  if (x.t != 1.f) { xi[nxw] = x.a0; xw[nxw++] = 1.f - x.t; }
+  if (x.t != 0.f) { xi[nxw] = x.a1; xw[nxw++] = x.t; }
+  if (y.t != 1.f) { yi[nyw] = y.a0; yw[nyw++] = 1.f - y.t; }
+  if (y.t != 0.f) { yi[nyw] = y.a1; yw[nyw++] = y.t; }
+  if (z.t != 1.f) { zi[nzw] = z.a0; zw[nzw++] = 1.f - z.t; }
+  if (z.t != 0.f) { zi[nzw] = z.a1; zw[nzw++] = z.t; }
+  float acc = 0.f;
+  for (int a = 0; a < nxw; a++)
+    for (int b = 0; b < nyw; b++) {
+      float zs = 0.f;
+      for (int q = 0; q < nzw; q++) zs += zw[q] * cget(eb, C, xi[a], yi[b], zi[q]);
+      acc += xw[a] * yw[b] * zs;
+    }
+  ef[fstride * blockIdx.y + (size_t)c * F.csz + s] += acc;
 }
 
 // Coarsest level: red-black SOR in shared memory, one CTA per problem, a
@@ -370,6 +489,147 @@ __global__ void k_init_vals(double* __restrict__ phi, const uint8_t* __restrict_
   phi[blockIdx.y * nstride + t] = fixed[t] ? val[blockIdx.y * nstride + t] : 0.0;
 }
 
+// ---- flexible CG on the FP32 correction (level 0, split layout) --------
+//
+// Solves L x = r with L = 6 - sum(neighbours) (the negated 7-point operator,
+// symmetric positive definite on the free nodes), preconditioned by the
+// multigrid cycle (z = V(g) with g = -r, since the cycle solves A e = g with
+// A = -L).  Flexible CG, one-term form: alpha = <p, r>/<p, L p>,
+// beta = -<z_new, L p_old>/<p_old, L p_old>.  The solver carries g = -r
+// instead of r.  Dot products: per-thread FP32 over four slots, per-block
+// FP64, then a fixed-order FP64 sum per problem (deterministic).
+
+__device__ __forceinline__ double block_sum_d(double v, double* sh) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x < 32) {
+    t = threadIdx.x < blockDim.x / 32 ? sh[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_xor_sync(0xffffffffu, t, o);
+  }
+  return t;  // valid in thread 0
+}
+
+// p = z + beta p on valid free slots (p stays 0 on metal).
+__global__ void __launch_bounds__(kT)
+k_cg_dir(float* __restrict__ p, const float* __restrict__ z,
+         const double* __restrict__ scal, size_t pstride, uint32_t n) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= n) return;
+  const float b = (float)scal[4 * blockIdx.y + 2];
+  const size_t o = blockIdx.y * pstride + t;
+  p[o] = z[o] + b * p[o];
+}
+
+// q = L p (both colours; q = 0 on metal) and block partials of <p, q> and
+// <p, g>; blockIdx.z = colour.
+__global__ void __launch_bounds__(kT)
+k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
+            const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ q,
+            double* __restrict__ part, size_t pstride) {
+  __shared__ double sh[kT / 32];
+  const int c = blockIdx.z;
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  const uint32_t nq = G.csz >> 2;
+  float spq = 0.f, spg = 0.f;
+  if (t < nq) {
+    const uint32_t ij = fdivu(t, G.dH4);
+    const int m0 = 4 * (int)(t - ij * G.dH4.d);
+    const int i = (int)fdivu(ij, G.dny);
+    const int j = (int)(ij - (uint32_t)i * G.dny.d);
+    const int pc = (i + j + c) & 1;
+    const uint32_t base = ij * (uint32_t)G.H + m0;
+    const float* pb = p + blockIdx.y * pstride;
+    const float* own = pb + (size_t)c * G.csz;
+    const float* oth = pb + (size_t)(1 - c) * G.csz;
+    const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + (size_t)c * G.csz + base);
+    const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
+    const float4 pv = ld4(own + base);
+    const float4 gv = ld4(g + blockIdx.y * pstride + (size_t)c * G.csz + base);
+    const float pp[4] = {pv.x, pv.y, pv.z, pv.w};
+    const float gg[4] = {gv.x, gv.y, gv.z, gv.w};
+    float out[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int k = 2 * (m0 + u) + pc;
+      out[u] = 0.f;
+      if (!mv[u] && k < G.nz)
+        out[u] = 6.0f * pp[u] - nbr_sum(G, own, oth, i, j, m0 + u, k, base + u);
+      spq += pp[u] * out[u];
+      spg += pp[u] * gg[u];
+    }
+    *reinterpret_cast<float4*>(q + blockIdx.y * pstride + (size_t)c * G.csz + base) =
+        make_float4(out[0], out[1], out[2], out[3]);
+  }
+  const double a = block_sum_d((double)spq, sh);
+  __syncthreads();
+  const double b = block_sum_d((double)spg, sh);
+  if (threadIdx.x == 0) {
+    const size_t slot = ((size_t)blockIdx.y * 2 + c) * gridDim.x + blockIdx.x;
+    part[2 * slot] = a;
+    part[2 * slot + 1] = b;
+  }
+}
+
+// block partials of <z, q>
+__global__ void __launch_bounds__(kT)
+k_cg_dot(const float* __restrict__ z, const float* __restrict__ q,
+         double* __restrict__ part, size_t pstride, uint32_t n) {
+  __shared__ double sh[kT / 32];
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  float s = 0.f;
+  if (t < n) {
+    const size_t o = blockIdx.y * pstride + t;
+    s = z[o] * q[o];
+  }
+  const double a = block_sum_d((double)s, sh);
+  if (threadIdx.x == 0) part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = a;
+}
+
+// Per-problem fixed-order sums of the partials.  mode 0: alpha from <p,q>
+// and <p,g> (also keeps <p,q> for beta); mode 1: beta = -<z,q>/<p,q>.
+// scal[4b + 0] = <p,q>, [1] = alpha, [2] = beta.
+__global__ void __launch_bounds__(kT)
+k_cg_reduce(const double* __restrict__ part, int nparts, int stride,
+            double* __restrict__ scal, int mode) {
+  __shared__ double sh[kT / 32];
+  const int b = blockIdx.x;
+  double a = 0.0, c = 0.0;
+  for (int k = threadIdx.x; k < nparts; k += blockDim.x) {
+    const size_t o = (size_t)b * nparts + k;
+    a += part[stride * o];
+    if (stride == 2) c += part[stride * o + 1];
+  }
+  const double sa = block_sum_d(a, sh);
+  __syncthreads();
+  const double sc = block_sum_d(c, sh);
+  if (threadIdx.x == 0) {
+    double* S = scal + 4 * b;
+    if (mode == 0) {
+      S[0] = sa;
+      S[1] = sa > 0.0 ? -sc / sa : 0.0;
+    } else {
+      S[2] = S[0] > 0.0 ? -sa / S[0] : 0.0;
+    }
+  }
+}
+
+// x += alpha p; g += alpha q
+__global__ void __launch_bounds__(kT)
+k_cg_update(float* __restrict__ x, float* __restrict__ g, const float* __restrict__ p,
+            const float* __restrict__ q, const double* __restrict__ scal,
+            size_t pstride, uint32_t n) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= n) return;
+  const float al = (float)scal[4 * blockIdx.y + 1];
+  const size_t o = blockIdx.y * pstride + t;
+  x[o] += al * p[o];
+  g[o] += al * q[o];
+}
+
 // ---- host side ----------------------------------------------------------
 
 #define MK(x)                                                                \
@@ -462,6 +722,13 @@ struct Session {
   Buf<uint8_t> stage;   // per-call staging of basis masks
   Buf<double> vstage;   // per-call staging of Dirichlet values
   Buf<unsigned long long> dmax;
+  // flexible CG state (level 0, split FP32): correction x, direction p,
+  // q = L p; dot-product partials and per-problem scalars
+  Buf<float> xb, pb, qb;
+  Buf<double> part, scal;
+  int method = 1;            // 0: defect correction with `vcycles` cycles,
+                             // 1: flexible CG preconditioned by one cycle
+  int cg_iters = 4;          // CG iterations per FP64 refinement
   int nu1 = 2, nu2 = 2, vcycles = 2, bottom_pairs = 40;
   int gamma = 1;             // 1: V-cycle, 2: W-cycle (coarse levels twice)
   float smooth_omega = 1.f;  // red-black relaxation factor of the smoother
@@ -477,6 +744,11 @@ struct Session {
     stage.release();
     vstage.release();
     dmax.release();
+    xb.release();
+    pb.release();
+    qb.release();
+    part.release();
+    scal.release();
     if (s) {
       cudaStreamSynchronize(s);
       cudaStreamDestroy(s);
@@ -507,6 +779,7 @@ struct Session {
       MK(cudaMemsetAsync(L.e.p, 0, L.pstride * bmax * 4, s));
       MK(cudaMemsetAsync(L.g.p, 0, L.pstride * bmax * 4, s));
       const bool bottom = is_bottom(c);
+      L.rstride = std::max<size_t>(L.G.n, L.G.csz);
       if (!bottom) L.r.alloc(L.rstride * bmax, s);
       lv.push_back(std::move(L));
       if (bottom) break;
@@ -515,6 +788,15 @@ struct Session {
     bottom_omega = (float)omega_of(lv.back().d);
     phi.alloc(n * bmax, s);
     dmax.alloc(bmax, s);
+    if (method == 1) {
+      const size_t ps = lv[0].pstride * bmax;
+      xb.alloc(ps, s);
+      pb.alloc(ps, s);
+      qb.alloc(ps, s);
+      const size_t nb4 = nblk(lv[0].G.csz / 4), nbn = nblk((uint32_t)lv[0].pstride);
+      part.alloc(std::max(4 * nb4, nbn) * bmax, s);
+      scal.alloc(4 * bmax, s);
+    }
     MK(cudaGetLastError());
   }
 
@@ -526,12 +808,19 @@ struct Session {
                                             bottom_pairs, a.pstride);
       return;
     }
+    const dim3 g4(nblk(a.G.csz / 4), B);
     for (int q = 0; q < nu1; q++)
       for (int c = 0; c < 2; c++)
-        k_gs<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, smooth_omega, a.pstride);
-    k_resid<<<gn, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p, a.pstride, a.rstride);
+        k_gs4<<<g4, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, smooth_omega, a.pstride);
     MLevel& b = lv[l + 1];
-    k_restrict<<<dim3(nblk(b.G.n), B), kT, 0, s>>>(a.r.p, a.G, b.g.p, b.G, a.rstride, b.pstride);
+    if (nu1 > 0 && smooth_omega == 1.f) {
+      // Gauss-Seidel ended on colour 1: its residual is zero
+      k_resid0<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p, a.pstride);
+      k_restrict0<<<dim3(nblk(b.G.n), B), kT, 0, s>>>(a.r.p, a.G, b.g.p, b.G, b.pstride);
+    } else {
+      k_resid<<<gn, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p, a.pstride, a.rstride);
+      k_restrict<<<dim3(nblk(b.G.n), B), kT, 0, s>>>(a.r.p, a.G, b.g.p, b.G, a.rstride, b.pstride);
+    }
     if (l + 2 < lv.size()) MK(cudaMemsetAsync(b.e.p, 0, b.pstride * B * 4, s));
     // the coarse correction: gamma cycles on the coarse equation (the
     // bottom is solved directly, so once is enough there)
@@ -541,7 +830,7 @@ struct Session {
     // post-smoothing in the reverse colour order keeps the cycle symmetric
     for (int q = 0; q < nu2; q++)
       for (int c = 1; c >= 0; c--)
-        k_gs<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, smooth_omega, a.pstride);
+        k_gs4<<<g4, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, smooth_omega, a.pstride);
   }
 
   // one refinement step: FP64 residual, V-cycles on the correction, update
@@ -556,6 +845,43 @@ struct Session {
     k_update64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.e.p, f.G, dmax.p, nstride, f.pstride);
   }
 
+  // the flexible CG: once per solve, the FP64 residual and zero state
+  void cg_init() {
+    MLevel& f = lv[0];
+    const dim3 gn(nblk(f.G.n), B);
+    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, f.G.n, f.pstride);
+    MK(cudaMemsetAsync(xb.p, 0, f.pstride * B * 4, s));
+    MK(cudaMemsetAsync(pb.p, 0, f.pstride * B * 4, s));
+    MK(cudaMemsetAsync(qb.p, 0, f.pstride * B * 4, s));
+    MK(cudaMemsetAsync(scal.p, 0, 4 * B * 8, s));
+  }
+
+  // cg_iters preconditioned iterations, then the reliable update: the FP32
+  // correction is added to the FP64 potential, whose exact FP64 residual
+  // replaces the carried one (the search direction is kept)
+  void cg_enqueue() {
+    MLevel& f = lv[0];
+    const uint32_t n = (uint32_t)f.pstride;
+    const dim3 gv(nblk(n), B);
+    const unsigned nb4 = nblk(f.G.csz / 4);
+    for (int it = 0; it < cg_iters; it++) {
+      MK(cudaMemsetAsync(f.e.p, 0, f.pstride * B * 4, s));
+      vcycle(0);  // z = f.e
+      k_cg_dot<<<gv, kT, 0, s>>>(f.e.p, qb.p, part.p, f.pstride, n);
+      k_cg_reduce<<<B, kT, 0, s>>>(part.p, (int)nblk(n), 1, scal.p, 1);
+      k_cg_dir<<<gv, kT, 0, s>>>(pb.p, f.e.p, scal.p, f.pstride, n);
+      k_cg_matvec<<<dim3(nb4, B, 2), kT, 0, s>>>(pb.p, f.g.p, f.mask.p, f.G, qb.p, part.p,
+                                                f.pstride);
+      k_cg_reduce<<<B, kT, 0, s>>>(part.p, 2 * (int)nb4, 2, scal.p, 0);
+      k_cg_update<<<gv, kT, 0, s>>>(xb.p, f.g.p, pb.p, qb.p, scal.p, f.pstride, n);
+    }
+    const dim3 gn(nblk(f.G.n), B);
+    MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
+    k_update64<<<gn, kT, 0, s>>>(phi.p, fixed.p, xb.p, f.G, dmax.p, f.G.n, f.pstride);
+    MK(cudaMemsetAsync(xb.p, 0, f.pstride * B * 4, s));
+    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, f.G.n, f.pstride);
+  }
+
   void step() {
     cudaGraphExec_t exec = nullptr;
     for (auto& g : graphs)
@@ -563,7 +889,10 @@ struct Session {
     if (!exec) {
       cudaGraph_t graph;
       MK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-      step_enqueue();
+      if (method == 1)
+        cg_enqueue();
+      else
+        step_enqueue();
       MK(cudaStreamEndCapture(s, &graph));
       MK(cudaGraphInstantiate(&exec, graph, 0));
       MK(cudaGraphDestroy(graph));
@@ -579,6 +908,7 @@ struct Session {
       const int reps = (l + 2 < (int)lv.size()) ? gamma : 1;
       c[l] = 2 * (nu1 + nu2) + 3 + reps * c[l + 1];
     }
+    if (method == 1) return 2 + cg_iters * (c[0] + 6);
     return 2 + c[0] * vcycles;
   }
 };
@@ -595,6 +925,7 @@ struct MixedResult {
 // about d_k * rho / (1 - rho) (a geometric tail).  A problem is done when
 // that bound and d_k itself are below acc.
 MixedResult run_mixed(Session& M, double acc, int max_steps) {
+  if (M.method == 1) M.cg_init();
   std::vector<unsigned long long> h(M.B);
   std::vector<double> prev(M.B, INFINITY);
   MixedResult res{IG_NOT_CONVERGED, 0, std::vector<double>(M.B, 0.0)};
@@ -653,13 +984,13 @@ int ig_mixed_open(const uint8_t* metal, long nx, long ny, long nz,
                   int max_problems, int stencil, int nu1, int nu2, int vcycles,
                   void** handle) {
   return ig_mixed_open_ex(metal, nx, ny, nz, max_problems, stencil, nu1, nu2,
-                          vcycles, 1, 1.0, handle);
+                          vcycles, 1, 1.0, 1, 4, handle);
 }
 
 int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
                      int max_problems, int stencil, int nu1, int nu2,
                      int vcycles, int gamma, double smooth_omega,
-                     void** handle) {
+                     int method, int cg_iters, void** handle) {
   set_last_error("");
   if (!handle || !metal) {
     set_last_error("null argument");
@@ -688,6 +1019,8 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
     S->vcycles = std::max(1, vcycles);
     S->gamma = std::min(2, std::max(1, gamma));
     S->smooth_omega = (float)std::min(1.9, std::max(0.5, smooth_omega));
+    S->method = method == 0 ? 0 : 1;
+    S->cg_iters = std::min(64, std::max(1, cg_iters));
     // the Shortley-Weller residual with unit legs is half the ghost_linear
     // one: scale it so the correction solves the same equation
     S->resid_scale = stencil == 0 ? 1.0 : 2.0;
@@ -713,16 +1046,16 @@ int ig_mixed_time_gs(void* handle, int n_problems, int pairs, double* ms_per_lau
   }
   try {
     MLevel& f = S->lv[0];
-    const dim3 gs(nblk(f.G.csz), n_problems);
+    const dim3 gs(nblk(f.G.csz / 4), n_problems);
     cudaEvent_t e0, e1;
     MK(cudaEventCreate(&e0));
     MK(cudaEventCreate(&e1));
     for (int c = 0; c < 2; c++)  // warm
-      k_gs<<<gs, kT, 0, S->s>>>(f.e.p, f.g.p, f.mask.p, f.G, c, 1.f, f.pstride);
+      k_gs4<<<gs, kT, 0, S->s>>>(f.e.p, f.g.p, f.mask.p, f.G, c, 1.f, f.pstride);
     MK(cudaEventRecord(e0, S->s));
     for (int q = 0; q < pairs; q++)
       for (int c = 0; c < 2; c++)
-        k_gs<<<gs, kT, 0, S->s>>>(f.e.p, f.g.p, f.mask.p, f.G, c, 1.f, f.pstride);
+        k_gs4<<<gs, kT, 0, S->s>>>(f.e.p, f.g.p, f.mask.p, f.G, c, 1.f, f.pstride);
     MK(cudaEventRecord(e1, S->s));
     MK(cudaEventSynchronize(e1));
     float ms = 0.f;

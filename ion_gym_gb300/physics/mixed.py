@@ -21,10 +21,13 @@ from ion_gym_gb300.physics.solver3d import (SolveNotConverged, stencil_code,
                                             _union)
 
 
-# Cycle shape of the FP32 correction solve: nu1/nu2 red-black smoothing
-# pairs before/after the coarse correction, `vcycles` cycles per FP64
-# refinement step, gamma 1 (V) or 2 (W), smoother relaxation factor.
-CYCLE = {"nu1": 2, "nu2": 2, "vcycles": 2, "gamma": 1, "smooth_omega": 1.0}
+# Method of the FP32 correction solve: method 1 = flexible CG preconditioned
+# by one multigrid cycle, cg_iters iterations per FP64 refinement; method 0 =
+# defect correction with `vcycles` cycles per refinement.  Cycle shape:
+# nu1/nu2 red-black smoothing pairs before/after the coarse correction,
+# gamma 1 (V) or 2 (W), smoother relaxation factor.
+CYCLE = {"nu1": 2, "nu2": 2, "vcycles": 2, "gamma": 1, "smooth_omega": 1.0,
+         "method": 1, "cg_iters": 4}
 
 
 def session_bytes(shape, max_problems):
@@ -43,7 +46,8 @@ class MixedSession:
     def __init__(self, metal, max_problems, stencil="ghost_linear",
                  nu1=CYCLE["nu1"], nu2=CYCLE["nu2"],
                  vcycles=CYCLE["vcycles"], gamma=CYCLE["gamma"],
-                 smooth_omega=CYCLE["smooth_omega"]):
+                 smooth_omega=CYCLE["smooth_omega"], method=CYCLE["method"],
+                 cg_iters=CYCLE["cg_iters"]):
         metal = np.asarray(metal, bool)
         self.shape = metal.shape
         self.max_problems = int(max_problems)
@@ -52,7 +56,8 @@ class MixedSession:
         st = _lib.lib().ig_mixed_open_ex(
             ptr(as_mask(metal)), *self.shape, self.max_problems,
             stencil_code(stencil), int(nu1), int(nu2), int(vcycles),
-            int(gamma), float(smooth_omega), ctypes.byref(self._h))
+            int(gamma), float(smooth_omega), int(method), int(cg_iters),
+            ctypes.byref(self._h))
         _lib.check(st, "MixedSession")
 
     def _outcome(self, st, steps, dmax, accuracy, span):
@@ -63,19 +68,33 @@ class MixedSession:
                 f"{accuracy:.1e} of the span {span:g} V (worst applied change "
                 f"{dmax.max():.3e} V)")
 
-    def solve_bases(self, masks, v_basis=1e4, accuracy=1e-9, max_steps=40):
-        """masks: sequence of (nx,ny,nz) bool -> array (B, nx, ny, nz)."""
-        B = len(masks)
-        stack = np.empty((B,) + self.shape, np.uint8)
-        for b, m in enumerate(masks):
-            stack[b] = np.asarray(m, bool)
-        phi = np.empty((B,) + self.shape)
+    def solve_bases(self, masks, v_basis=1e4, accuracy=1e-9, max_steps=40,
+                    out=None):
+        """masks: sequence of (nx,ny,nz) bool, or a CUDA uint8 tensor
+        (B, nx, ny, nz) already on the device -> potentials (B, nx, ny, nz)
+        float64: a numpy array, or `out` (a CUDA float64 tensor) when
+        given."""
+        if type(masks).__module__.startswith("torch"):
+            B = int(masks.shape[0])
+            mptr = ctypes.c_void_p(masks.data_ptr())
+        else:
+            B = len(masks)
+            stack = np.empty((B,) + self.shape, np.uint8)
+            for b, m in enumerate(masks):
+                stack[b] = np.asarray(m, bool)
+            mptr = ptr(stack)
+        if out is None:
+            phi = np.empty((B,) + self.shape)
+            pptr = ptr(phi)
+        else:
+            phi = out
+            pptr = ctypes.c_void_p(out.data_ptr())
         steps = ctypes.c_int(0)
         dmax = np.zeros(B)
         span = abs(float(v_basis))
         st = _lib.lib().ig_mixed_solve_bases(
-            self._h, ptr(stack), B, float(v_basis), float(accuracy) * span,
-            int(max_steps), ptr(phi), ctypes.byref(steps), ptr(dmax))
+            self._h, mptr, B, float(v_basis), float(accuracy) * span,
+            int(max_steps), pptr, ctypes.byref(steps), ptr(dmax))
         self._outcome(st, steps.value, dmax, accuracy, span)
         self.last_steps = int(steps.value)
         return phi

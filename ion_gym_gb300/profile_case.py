@@ -44,14 +44,46 @@ def sweep_f64(n, pairs):
           f"last max|d| {d.value:.3e}")
 
 
+def mixed_rings(solves, gs_pairs):
+    """One resident session of the 193x193x385 ring stack (8 bases + the
+    grounded box as metal): `solves` mixed solves to 1e-9 of the span, then
+    `gs_pairs` timed pairs of the fine-level FP32 smoother alone."""
+    import torch
+    from ion_gym_gb300 import _lib
+    from ion_gym_gb300.workloads import ring_stack
+    from ion_gym_gb300.physics.mixed import MixedSession
+    masks, box = ring_stack(0)
+    metal = box.copy()
+    for m in masks.values():
+        metal |= m
+    rings = [masks[i] for i in sorted(masks)]
+    with MixedSession(metal, len(rings)) as s:
+        for _ in range(solves):
+            t0 = time.perf_counter()
+            s.solve_bases(rings, 1e4, 1e-9)
+            print(f"mixed_rings: 8 bases in {time.perf_counter() - t0:.3f} s, "
+                  f"{s.last_steps} refinement steps")
+        if gs_pairs:
+            ms = ctypes.c_double(0)
+            by = ctypes.c_double(0)
+            _lib.lib().ig_mixed_time_gs(s._h, len(rings), gs_pairs,
+                                        ctypes.byref(ms), ctypes.byref(by))
+            print(f"k_gs: {ms.value * 1e3:.1f} us per launch, "
+                  f"{by.value / (ms.value * 1e-3) / 1e9:.0f} GB/s algorithmic")
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["sweep_f64"])
+    ap.add_argument("case", choices=["sweep_f64", "mixed_rings"])
     ap.add_argument("--n", type=int, default=257)
     ap.add_argument("--pairs", type=int, default=4)
+    ap.add_argument("--solves", type=int, default=1)
     a = ap.parse_args()
     if a.case == "sweep_f64":
         sweep_f64(a.n, a.pairs)
+    else:
+        mixed_rings(a.solves, a.pairs)
 
 
 if __name__ == "__main__":
