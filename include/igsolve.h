@@ -157,6 +157,9 @@ int ig_mixed_bases(const uint8_t *metal, const uint8_t *masks, int n_bases,
  * session's metal, problem p with the values vals[p] (float64 (n) each) at
  * the metal nodes.  Arrays may be host or device memory. */
 long ig_mixed_bytes(long nx, long ny, long nz, int max_problems);
+/* Kernel launches the mixed path has issued (graph replays counted node by
+ * node) since the library was loaded. */
+long ig_mixed_launch_count(void);
 int ig_mixed_open(const uint8_t *metal, long nx, long ny, long nz,
                   int max_problems, int stencil, int nu1, int nu2, int vcycles,
                   void **handle);
@@ -212,6 +215,28 @@ int ig_cascadic_relres_noalloc(const uint8_t *fixed, const double *val,
                                long *sweeps_out, double *relres_out,
                                long *total_pairs_out, int *levels_out,
                                void *stream);
+
+/* ---- analytic scenes (physics/rasterize3d.py, physics/solver3d.py) ------
+ * A scene is a primitive table in grid units, 16 doubles per row: kind
+ * (0 z-cylinder, 1 box), electrode slot (rows in slot order), shape id,
+ * role (0 within, 1 notin), six bounds with +1e-9 (inclusive) and six with
+ * -1e-9 (strict): cylinder cx, cy, r^2+e, (z-length)-e, z+e, 0; box x1-e,
+ * x2+e, y1-e, y2+e, z1-e, z2+e.
+ * ig_rasterize (rasterize3d.py:45-109): int16 labels (electrode_index[slot]
+ * inside, 0 vacuum), per slot the node count, the count of nodes it claims
+ * from an earlier electrode and the lowest such flat index.
+ * ig_theta_scene (solver3d.py:75-127): theta (6, nx, ny, nz) float32 of
+ * every vacuum node whose neighbour along a direction is metal, by `iters`
+ * bisections of the exact inside test; mirror_bits: bit a set = low mirror
+ * plane on axis a. */
+int ig_rasterize(const double *table, int n_prims, const int *electrode_index,
+                 int n_electrodes, long nx, long ny, long nz,
+                 int16_t *labels_out, unsigned long long *counts_out,
+                 unsigned long long *clash_counts_out,
+                 unsigned long long *clash_first_out);
+int ig_theta_scene(const double *table, int n_prims, const uint8_t *metal,
+                   long nx, long ny, long nz, int mirror_bits, int iters,
+                   float *theta_out);
 
 /* ---- single kernels on device arrays ----------------------------------- */
 

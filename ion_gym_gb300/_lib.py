@@ -67,6 +67,7 @@ SIGNATURES = {
     "ig_mixed_bases": (_i, [_p, _p, _i, _d, _l, _l, _l, _i, _d, _i, _i, _i,
                             _i, _p, _pi, _p]),
     "ig_mixed_bytes": (_l, [_l, _l, _l, _i]),
+    "ig_mixed_launch_count": (_l, []),
     "ig_mixed_open": (_i, [_p, _l, _l, _l, _i, _i, _i, _i, _i,
                            ctypes.POINTER(ctypes.c_void_p)]),
     "ig_mixed_open_ex": (_i, [_p, _l, _l, _l, _i, _i, _i, _i, _i, _i, _d,
@@ -74,6 +75,8 @@ SIGNATURES = {
     "ig_mixed_solve_bases": (_i, [_p, _p, _i, _d, _d, _i, _p, _pi, _p]),
     "ig_mixed_solve_values": (_i, [_p, _p, _i, _d, _i, _p, _pi, _p]),
     "ig_mixed_close": (None, [_p]),
+    "ig_rasterize": (_i, [_p, _i, _p, _i, _l, _l, _l, _p, _p, _p, _p]),
+    "ig_theta_scene": (_i, [_p, _i, _p, _l, _l, _l, _i, _i, _p]),
     "ig_mixed_time_gs": (_i, [_p, _i, _i, _pd, _pd]),
     "ig_cascadic_relres_noalloc": (_i, [_p, _p, _l, _l, _l, _d, _l, _i, _i,
                                         _d, _p, _i, _i, _p, _pl, _pd, _pl,

@@ -975,6 +975,8 @@ using namespace ig;
 
 extern "C" {
 
+long ig_mixed_launch_count(void) { return mixed_launch_total(); }
+
 long ig_mixed_bytes(long nx, long ny, long nz, int max_problems) {
   if (nx < 1 || ny < 1 || nz < 1 || max_problems < 1) return -1;
   return (long)session_bytes(Dims{nx, ny, nz}, max_problems);

@@ -399,10 +399,55 @@ def cache_cases():
     return out
 
 
+def raster_cases():
+    """physics/rasterize3d.rasterize on small analytic scenes, and the
+    messages of its two refusals (overlapping electrodes, an electrode with
+    no node)."""
+    from ion_gym.physics.scene3d import (GeomScene, GridSpec, Electrode,
+                                         Shape, Cylinder, Box3D)
+    from ion_gym.physics.rasterize3d import rasterize
+    out = {}
+    g = GridSpec(31, 29, 27, mm_per_gu=0.5, overhang="allow")
+    scenes = [
+        GeomScene(grid=g, units="mm", electrodes=[
+            Electrode(1, "rod", [Shape([Cylinder(7.5, 7.0, 12.0, 2.35, 9.0)])]),
+            Electrode(3, "plate", [Shape(
+                within=[Box3D(1.0, 1.0, 1.2, 14.0, 3.3, 2.1)],
+                notin=[Cylinder(7.5, 2.0, 3.0, 1.1, 4.0)])]),
+            Electrode(2, "cup", [Shape(
+                within=[Cylinder(7.5, 7.0, 13.0, 6.4, 2.0)],
+                notin=[Cylinder(7.5, 7.0, 13.0, 5.2, 2.0)])])]),
+        GeomScene(grid=GridSpec(25, 23, 9, overhang="allow"), units="gu",
+                  electrodes=[
+            Electrode(1, "a", [Shape([Box3D(2.0, 2.0, 0.0, 10.0, 20.0, 8.0)]),
+                               Shape([Cylinder(18.0, 11.0, 8.0, 4.5, 8.0)])]),
+            Electrode(2, "b", [Shape([Box3D(12.5, 0.0, 0.0, 13.5, 22.0,
+                                            8.0)])])]),
+    ]
+    for idx, sc in enumerate(scenes):
+        out[f"raster/{idx}/lab"] = rasterize(sc)
+    clash = GeomScene(grid=GridSpec(20, 20, 5, overhang="allow"), units="gu",
+                      electrodes=[
+        Electrode(1, "a", [Shape([Box3D(2.0, 2.0, 0.0, 10.0, 10.0, 4.0)])]),
+        Electrode(2, "b", [Shape([Box3D(8.0, 8.0, 0.0, 15.0, 15.0, 4.0)])])])
+    empty = GeomScene(grid=GridSpec(20, 20, 5, overhang="allow"), units="gu",
+                      electrodes=[
+        Electrode(1, "a", [Shape([Box3D(2.0, 2.0, 0.0, 10.0, 10.0, 4.0)])]),
+        Electrode(2, "tiny", [Shape([Cylinder(15.5, 15.5, 2.5, 0.2, 0.3)])])])
+    for name, sc in (("clash", clash), ("empty", empty)):
+        try:
+            rasterize(sc)
+            raise AssertionError(f"{name}: no refusal")
+        except ValueError as e:
+            out[f"raster_err/{name}/message"] = np.array(str(e))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
-    ap.add_argument("--only", choices=["kernels", "drivers", "theta", "cache"],
+    ap.add_argument("--only", choices=["kernels", "drivers", "theta", "cache",
+                                       "raster"],
                     default=None)
     a = ap.parse_args()
     import ion_gym.physics.solver3d as S
@@ -424,6 +469,10 @@ def main():
     if a.only in (None, "cache"):
         np.savez_compressed(os.path.join(a.out, "cache.npz"), **cache_cases())
         print("cache.npz written")
+    if a.only in (None, "raster"):
+        np.savez_compressed(os.path.join(a.out, "raster.npz"),
+                            **raster_cases())
+        print("raster.npz written")
 
 
 if __name__ == "__main__":
