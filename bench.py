@@ -544,6 +544,158 @@ def run_serve(a):
         "basis_solves_s": bases / el}), flush=True)
 
 
+def run_compose(a):
+    """The field build after a ring-stack basis solve (193x193x385, 8 unit
+    bases): static field plus 3 drive channels, each potential composed
+    from the bases and its electrode-aware E-field, all resident.  e2e is
+    the reference-facing call with host bases in and host float64 channels
+    out."""
+    import torch
+    from ion_gym_gb300 import _lib
+    from ion_gym_gb300.workloads import ring_stack, ring_stack_drive
+    from ion_gym_gb300.physics import field3d
+    torch.cuda.set_device(0)
+    L = _lib.lib()
+    masks, box = ring_stack(0)
+    shape = box.shape
+    n = box.size
+    lab = np.zeros(shape, np.int16)
+    for i, m in masks.items():
+        lab[m] = i
+    lab[box] = 9
+    spec = ring_stack_drive(len(masks))
+    g = torch.Generator(device="cuda").manual_seed(11)
+    # unit bases as the device basis door leaves them: rows 16-byte aligned
+    stack = field3d.padded(len(masks), shape)
+    for r in range(len(masks)):
+        stack[r].copy_(torch.rand(shape, generator=g, device="cuda",
+                                  dtype=torch.float32))
+    bases_d = {i + 1: stack[i] for i in range(len(masks))}
+    ele_d = torch.from_numpy(lab).cuda()
+    plan, _ = field3d.drive_plan(spec, bases_d)
+    nch, nsteps = plan["weights"].shape
+    # per-kernel event timing on the launching (current) stream: the C-ABI
+    # calls with every argument prepared, R launches between two events
+    st = torch.cuda.current_stream()
+    for _ in range(a.warmup):
+        field3d.compose_drive_channels(spec, bases_d, ele_d)
+    import ctypes
+    keys = plan["keys"]
+    ptrs = (ctypes.c_void_p * nsteps)(*[bases_d[keys[r]].data_ptr()
+                                       for r in plan["rows"]])
+    w = np.ascontiguousarray(plan["weights"], np.float32)
+    mu = np.ascontiguousarray(plan["mult"], np.uint8)
+    P = field3d.padded(nch, shape)
+    E = torch.empty((3, nch) + shape, dtype=torch.float32, device="cuda")
+    metal_d = (ele_d != 0).to(torch.uint8)
+    sh = ctypes.c_void_p(st.cuda_stream)
+    h = spec.geometry.mm_per_gu
+
+    def sup():
+        return L.ig_superpose_dev(ptrs, nsteps, nch, _lib.ptr(w), _lib.ptr(mu), n,
+                                  ctypes.c_void_p(P.data_ptr()), P.stride(0), sh)
+
+    def fld():
+        return L.ig_field_aware_dev(
+            ctypes.c_void_p(P.data_ptr()), 0, P.stride(0), nch,
+            ctypes.c_void_p(metal_d.data_ptr()), *shape, float(h), 0,
+            ctypes.c_void_p(E[0].data_ptr()), ctypes.c_void_p(E[1].data_ptr()),
+            ctypes.c_void_p(E[2].data_ptr()), E.stride(1), sh)
+
+    def fld_plain():
+        return L.ig_field_aware_dev(
+            ctypes.c_void_p(P.data_ptr()), 0, P.stride(0), nch, None, *shape,
+            float(h), 0, ctypes.c_void_p(E[0].data_ptr()),
+            ctypes.c_void_p(E[1].data_ptr()), ctypes.c_void_p(E[2].data_ptr()),
+            E.stride(1), sh)
+
+    R = 10
+    times = {}
+    for name, fn in (("sup", sup), ("fld", fld), ("plain", fld_plain)):
+        assert fn() == 0, _lib.last_error()
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+        ev[0].record(st)
+        for _ in range(R):
+            fn()
+        ev[1].record(st)
+        ev[1].synchronize()
+        times[name] = ev[0].elapsed_time(ev[1]) / R
+    t_sup, t_fld = times["sup"] * a.steps, times["fld"] * a.steps
+    del P, E
+    clocks = Clocks(0)
+    launches0 = L.ig_launch_count()
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(a.steps):
+        ch = field3d.compose_drive_channels(spec, bases_d, ele_d)
+    e1.record(st)
+    e1.synchronize()
+    el = e0.elapsed_time(e1) * 1e-3
+    ck = clocks.stop()
+    launches = L.ig_launch_count() - launches0
+    del ch
+    # e2e: host bases in, host float64 channels out
+    bases_h = {i: stack[i - 1].cpu().numpy() for i in bases_d}
+    t1 = time.perf_counter()
+    for _ in range(a.steps):
+        ch = field3d.compose_drive_channels(spec, bases_h, lab)
+    el_e2e = time.perf_counter() - t1
+    d2h = sum(v.nbytes for k, v in ch.items() if isinstance(v, np.ndarray))
+    d2h += sum(v.nbytes for v in ch["chan_phi"])
+    del ch
+    sup_b = n * 4 * (nsteps + nch)
+    fld_b = n * (1 + nch * 16)
+    sup_gbs = sup_b / (t_sup / a.steps * 1e-3) / 1e9
+    fld_gbs = fld_b / (t_fld / a.steps * 1e-3) / 1e9
+    peak = _peak()
+    dom = ("k_field32 (electrode-aware gradient, metal rule fused)", fld_gbs, fld_b,
+           t_fld) if t_fld >= t_sup else ("k_superpose (drive superposition)",
+                                          sup_gbs, sup_b, t_sup)
+    line = {
+        "metric": "composes/s (static + 3 drive channels, fields)",
+        "value": a.steps / el, "unit": "composes/s", "n_gpus": 1,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32", "data": "synthetic (seeded ring stack, random bases)",
+        "config": {"workload": "compose_ring_stack_193x193x385_8_bases_4_channels",
+                   "grid": list(shape), "bases": len(masks), "channels": nch,
+                   "l2": "inputs larger than L2"},
+        "e2e": {"value": a.steps / el_e2e, "unit": "composes/s",
+                "h2d_bytes_per_step": n * 4 * len(masks) + n * 2,
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "kernels": {"k_superpose": {"GB/s": sup_gbs, "us": 1e3 * t_sup / a.steps,
+                                    "bytes": sup_b},
+                    "k_field32": {"GB/s": fld_gbs,
+                                               "us": 1e3 * t_fld / a.steps,
+                                               "bytes": fld_b},
+                    "k_field32 without a metal mask": {
+                        "us": 1e3 * times["plain"],
+                        "GB/s": (fld_b - n) / (times["plain"] * 1e-3) / 1e9}},
+        "roofline": {"bound": "hbm", "achieved": dom[1], "peak": peak,
+                     "unit": "GB/s", "frac": dom[1] / peak if peak else None,
+                     "traffic": None, "kernel": dom[0],
+                     "avg_launch_us": 1e3 * dom[3] / a.steps},
+        "clocks": ck,
+    }
+    if not a.no_cpu:
+        from oracle import field as F
+        b0 = bases_h[1]
+        t = time.perf_counter()
+        F.field_aware_3d(b0, lab, spec.geometry.mm_per_gu, False, True)
+        tc = time.perf_counter() - t
+        line["cpu_baseline"] = {
+            "value": 1.0 / (tc * nch), "unit": "composes/s", "cores": 1,
+            "kind": "port",
+            "sample": f"one channel's electrode-aware field by the numpy "
+                      f"restatement in oracle/ ({tc:.1f} s), scaled to "
+                      f"{nch} channels; superposition not counted"}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -551,7 +703,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="quad257",
-                    choices=["quad257", "rings", "uneven", "serve"])
+                    choices=["quad257", "rings", "uneven", "serve",
+                             "compose"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--rate", type=float, default=20.0)
@@ -566,6 +719,8 @@ def main():
         run_uneven(a)
     elif a.workload == "serve":
         run_serve(a)
+    elif a.workload == "compose":
+        run_compose(a)
     else:
         run_ours(a)
 

@@ -238,6 +238,65 @@ int ig_theta_scene(const double *table, int n_prims, const uint8_t *metal,
                    long nx, long ny, long nz, int mirror_bits, int iters,
                    float *theta_out);
 
+/* ---- fields from solved bases ------------------------------------------ *
+ * Unit bases, drive superposition and the electrode-aware E-field, the same
+ * bits as the reference.
+ * ig_unit_bases_dev (build_stl3d.py:849): out = float32(phi / v_basis),
+ * float64 division rounded to float32.
+ * ig_superpose_dev / the first half of ig_compose_fields (build_stl3d.py:
+ * 547-568): a plan of n_steps steps in electrode order; step s reads the
+ * device basis basis_ptrs[s] (a host array of n_steps device pointers; in
+ * ig_compose_fields, row rows[s] of the host stack); channel c starts at +0
+ * and adds mult[c*n_steps+s] times float32(weights[c*n_steps+s] * basis),
+ * float32 round to nearest, no fused multiply-add.  The static drive A is a
+ * channel with weights float32(dc_i) (mult 0 where dc_i is 0); a drive
+ * group is a channel with weight 1 and mult = how often the electrode names
+ * the group.  Launches of IG_FIELD_MAX_CHANNELS channels by
+ * IG_FIELD_MAX_STEPS steps; longer plans continue the float32 sums.
+ * ig_field_aware_3d / ig_field_aware_dev (tracer3d.py:55-117): E = -grad
+ * phi on the node grid, numpy.gradient (central inside, first order at the
+ * faces) and, where metal is given, the one-sided difference into the
+ * vacuum at metal nodes with vacuum on exactly one side along an axis.
+ * dtype 0: float32 potential and fields, 1: float64.  h_is_f64 = 0 when the
+ * reference's spacing is a Python float (float32 potentials then divide in
+ * float32 by float32(2h) and float32(h)), 1 when it is a numpy float64
+ * (float64 division, rounded).  The metal rule divides in float64.  Every
+ * axis needs at least 2 nodes.  The _dev form does n_channels potentials
+ * phi_stride elements apart into fields out_stride apart.
+ * ig_compose_fields: host buffers; bases (n_bases, nx, ny, nz) float32 ->
+ * per channel its potential phi_out and ex/ey/ez_out (n_channels, nx, ny,
+ * nz) float32. */
+#define IG_FIELD_MAX_STEPS 64
+#define IG_FIELD_MAX_CHANNELS 8
+int ig_unit_bases_dev(const double *phi, long long n, double v_basis,
+                      float *out, void *stream);
+int ig_superpose_dev(const float *const *basis_ptrs, int n_steps,
+                     int n_channels, const float *weights,
+                     const uint8_t *mult, long long n, float *out,
+                     long long out_stride, void *stream);
+int ig_field_aware_dev(const void *phi, int dtype, long long phi_stride,
+                       int n_channels, const uint8_t *metal, long nx, long ny,
+                       long nz, double h, int h_is_f64, void *ex, void *ey,
+                       void *ez, long long out_stride, void *stream);
+int ig_field_aware_3d(const void *phi, int dtype, const uint8_t *metal,
+                      long nx, long ny, long nz, double h, int h_is_f64,
+                      void *ex, void *ey, void *ez);
+/* Self-check (no reference counterpart): the field kernels divide without
+ * the hardware division on their fast path (an FMA-corrected float32
+ * quotient; a float32 emulation of the float64 quotient with an exact
+ * fallback).  Compares them with the IEEE divisions for the spacing h:
+ * every float32 numerator over float32(h) and float32(2h), and `samples`
+ * hashed numerators over the float64 h and 2h.  *mismatches_out = the
+ * number of differing results (0 expected). */
+int ig_field_check_division(double h, unsigned long long samples,
+                            unsigned seed, unsigned long long *mismatches_out);
+int ig_compose_fields(const float *bases, int n_bases, int n_steps,
+                      const int *rows, int n_channels, const float *weights,
+                      const uint8_t *mult, const uint8_t *metal, long nx,
+                      long ny, long nz, double h, int h_is_f64,
+                      float *phi_out, float *ex_out, float *ey_out,
+                      float *ez_out);
+
 /* ---- single kernels on device arrays ----------------------------------- */
 
 /* solver3d._sweep (solver3d.py:131-198); theta NULL = all ones.  The max

@@ -25,6 +25,7 @@ _p = ctypes.c_void_p
 _d = ctypes.c_double
 _l = ctypes.c_long
 _i = ctypes.c_int
+_ll = ctypes.c_longlong
 _pl = ctypes.POINTER(ctypes.c_long)
 _pd = ctypes.POINTER(ctypes.c_double)
 _pi = ctypes.POINTER(ctypes.c_int)
@@ -77,6 +78,15 @@ SIGNATURES = {
     "ig_mixed_close": (None, [_p]),
     "ig_rasterize": (_i, [_p, _i, _p, _i, _l, _l, _l, _p, _p, _p, _p]),
     "ig_theta_scene": (_i, [_p, _i, _p, _l, _l, _l, _i, _i, _p]),
+    "ig_unit_bases_dev": (_i, [_p, _ll, _d, _p, _p]),
+    "ig_superpose_dev": (_i, [_p, _i, _i, _p, _p, _ll, _p, _ll, _p]),
+    "ig_field_aware_dev": (_i, [_p, _i, _ll, _i, _p, _l, _l, _l, _d, _i, _p,
+                                _p, _p, _ll, _p]),
+    "ig_field_aware_3d": (_i, [_p, _i, _p, _l, _l, _l, _d, _i, _p, _p, _p]),
+    "ig_field_check_division": (_i, [_d, ctypes.c_ulonglong, ctypes.c_uint,
+                                     _p]),
+    "ig_compose_fields": (_i, [_p, _i, _i, _p, _i, _p, _p, _p, _l, _l, _l,
+                               _d, _i, _p, _p, _p, _p]),
     "ig_mixed_time_gs": (_i, [_p, _i, _i, _pd, _pd]),
     "ig_cascadic_relres_noalloc": (_i, [_p, _p, _l, _l, _l, _d, _l, _i, _i,
                                         _d, _p, _i, _i, _p, _pl, _pd, _pl,

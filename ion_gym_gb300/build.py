@@ -23,7 +23,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
 # of their explicit round-to-nearest intrinsics
 EXTRA = {"ig_f64.cu": ["--fmad=false"]}
 SOURCES = ["ig_f64.cu", "ig_f32.cu", "ig_solvers.cu", "ig_mixed.cu",
-           "ig_noalloc.cu", "ig_geometry.cu"]
+           "ig_noalloc.cu", "ig_geometry.cu", "ig_field.cu"]
 
 
 def nvcc():

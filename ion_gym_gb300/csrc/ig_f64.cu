@@ -21,6 +21,7 @@ namespace ig {
 
 std::atomic<long> g_launches{0};
 long launch_total() { return g_launches.load(); }
+void note_launches(long n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
 namespace {
 

@@ -101,6 +101,8 @@ void launch_fill_ones_f32(cudaStream_t s, float* a, size_t n);
 
 // Number of kernel launches this library has issued since it was loaded.
 long launch_total();
+// Adds n launches issued by another translation unit to that count.
+void note_launches(long n);
 
 // Sets the calling thread's ig_last_error() message.
 void set_last_error(const std::string& m);

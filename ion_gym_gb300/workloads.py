@@ -150,3 +150,63 @@ def planar_board(seed, shape=(512, 128, 96), n_electrodes=16, layers=2,
     box = np.zeros(shape, bool)
     _box_faces(box)
     return masks, box
+
+
+class DriveGroup:
+    """One declared drive group (the attributes the composer reads)."""
+
+    def __init__(self, name, amplitude_v=0.0, offset_v=0.0, waveform="sin",
+                 frequency_hz=1.0e6, phase_deg=0.0, duty=0.5, interp="hold",
+                 table_t_us=(), table_v=()):
+        self.name, self.amplitude_v, self.offset_v = name, amplitude_v, offset_v
+        self.waveform, self.frequency_hz, self.phase_deg = (waveform,
+                                                            frequency_hz,
+                                                            phase_deg)
+        self.duty, self.interp = duty, interp
+        self.table_t_us, self.table_v = list(table_t_us), list(table_v)
+
+
+class DriveElectrode:
+    def __init__(self, name, groups=(), dc=0.0):
+        self.name, self._groups, self.dc = name, list(groups), dc
+
+    def group_names(self):
+        return list(self._groups)
+
+
+class DriveGeometry:
+    def __init__(self, rf_groups, electrodes, mm_per_gu, field_method=
+                 "electrode_aware", channel_dtype="float64"):
+        self.rf_groups, self.electrodes = rf_groups, electrodes
+        self.mm_per_gu, self.field_method = mm_per_gu, field_method
+        self.channel_dtype = channel_dtype
+
+
+class DriveSpec:
+    """The spec surface compose_drive_channels reads: .geometry and
+    dc_effective(electrode)."""
+
+    def __init__(self, geometry):
+        self.geometry = geometry
+
+    def dc_effective(self, el):
+        return el.dc
+
+
+def ring_stack_drive(n_rings=8, mm_per_gu=0.1, seed=0):
+    """Drive of a ring stack: alternate rings on two RF groups 180 degrees
+    apart (1.1 MHz, 150 V), a DC ladder on every ring and a table-waveform
+    gate on ring 1 -- three drive channels plus the static field."""
+    rng = np.random.default_rng(seed)
+    groups = [DriveGroup("rf_a", amplitude_v=150.0, frequency_hz=1.1e6),
+              DriveGroup("rf_b", amplitude_v=150.0, frequency_hz=1.1e6,
+                         phase_deg=180.0),
+              DriveGroup("gate", amplitude_v=40.0, waveform="table",
+                         table_t_us=(0.0, 2.0, 2.5, 10.0),
+                         table_v=(0.0, 0.0, 1.0, 1.0))]
+    els = []
+    for e in range(n_rings):
+        gr = ["rf_a" if e % 2 == 0 else "rf_b"] + (["gate"] if e == 0 else [])
+        els.append(DriveElectrode(f"ring{e + 1}", gr,
+                                  float(np.round(rng.uniform(-20, 20), 3))))
+    return DriveSpec(DriveGeometry(groups, els, mm_per_gu))

@@ -37,7 +37,8 @@ class Golden:
         self.by = {}
         for key in self.z.files:
             kind, idx, field = key.split("/")
-            self.by.setdefault(kind, {}).setdefault(int(idx), {})[field] = key
+            idx = int(idx) if idx.isdigit() else idx
+            self.by.setdefault(kind, {}).setdefault(idx, {})[field] = key
 
     def cases(self, kind):
         out = []

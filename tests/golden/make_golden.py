@@ -20,6 +20,9 @@ Fixture files:
   drivers.npz  whole solves (solve3d, solve3d_mg, solve3d_vmg, solve_bases,
                solve_bases_mg) with their returned (phi, sweeps, delta) and
                the messages of the refusals.
+  field.npz    tracer3d.build_field_aware_3d and
+               build_stl3d.compose_drive_channels on small grids, with the
+               messages of the composer's refusals.
 """
 import argparse
 import os
@@ -443,11 +446,168 @@ def raster_cases():
     return out
 
 
+class _El:
+    """Electrode stand-in with the two attributes the composer reads."""
+
+    def __init__(self, name, groups, dc):
+        self.name, self._groups, self.dc = name, list(groups), dc
+
+    def group_names(self):
+        return list(self._groups)
+
+
+class _Spec:
+    """SimSpec stand-in: .geometry and dc_effective(el)."""
+
+    def __init__(self, geometry):
+        self.geometry = geometry
+
+    def dc_effective(self, el):
+        return el.dc
+
+
+def _group(name, **kw):
+    from types import SimpleNamespace
+    d = dict(name=name, amplitude_v=0.0, offset_v=0.0, waveform="sin",
+             frequency_hz=1.0e6, phase_deg=0.0, duty=0.5)
+    d.update(kw)
+    return SimpleNamespace(**d)
+
+
+def _smooth(rng, shape, scale=1.0):
+    x = rng.standard_normal(shape)
+    for ax in range(3):
+        x = (x + np.roll(x, 1, ax) + np.roll(x, -1, ax)) / 3.0
+    return (scale * x).astype(np.float32)
+
+
+def _labels(rng, shape, boxes):
+    lab = np.zeros(shape, np.int16)
+    for idx, (lo, hi) in enumerate(boxes, start=1):
+        lab[tuple(slice(a, b) for a, b in zip(lo, hi))] = idx
+    return lab
+
+
+def field_specs():
+    """(name, geometry kwargs, electrodes) of the composer cases."""
+    from types import SimpleNamespace
+    ga = [_group("rf_a", amplitude_v=150.0, frequency_hz=1.1e6),
+          _group("rf_b", amplitude_v=150.0, waveform="cos", phase_deg=180.0,
+                 frequency_hz=1.1e6),
+          _group("sq", amplitude_v=0.0, offset_v=5.0, waveform="square",
+                 duty=0.3, frequency_hz=2.5e5),
+          _group("tab", amplitude_v=20.0, waveform="table", interp="linear",
+                 table_t_us=[0.0, 1.5, 3.0], table_v=[0.0, 1.0, -0.5]),
+          _group("idle", amplitude_v=0.0)]
+    ea = [_El("e1", ["rf_a"], 10.0), _El("e2", ["rf_b"], 0.0),
+          _El("e3", ["rf_a"], -3.25), _El("e4", ["sq", "tab"], 0.1),
+          _El("e5", ["tab", "idle"], 7e-3)]
+    gb = [_group("p", amplitude_v=75.5, phase_deg=33.0, frequency_hz=7.7e5),
+          _group("hold", amplitude_v=3.0, waveform="table",
+                 table_t_us=[0.0, 2.0], table_v=[1.0, 1.0])]
+    eb = [_El("a", ["p", "p"], 0.0), _El("b", [], 12.5),
+          _El("c", ["hold"], -1.0), _El("d", ["p"], 0.0)]
+    return [
+        ("aware_f64", dict(mm_per_gu=0.2), ga, ea),
+        ("plain_f32", dict(mm_per_gu=np.float64(0.15), field_method="plain",
+                           channel_dtype="float32"), ga, ea),
+        ("repeat_f64", dict(mm_per_gu=0.35), gb, eb),
+        ("static_only", dict(mm_per_gu=0.5), [], [_El("x", [], 2.0),
+                                                  _El("y", [], 0.0)]),
+    ]
+
+
+def field_error_specs():
+    ok = [_El("e1", ["g"], 1.0), _El("e2", [], 0.0)]
+    return [
+        ("undefined", [_group("g", amplitude_v=1.0)],
+         [_El("e1", ["nope"], 0.0), _El("e2", [], 0.0)]),
+        ("unused", [_group("g", amplitude_v=1.0), _group("h", offset_v=2.0)],
+         ok),
+        ("waveform", [_group("g", amplitude_v=1.0, waveform="saw")], ok),
+        ("duty", [_group("g", amplitude_v=1.0, waveform="square", duty=1.0)],
+         ok),
+        ("table", [_group("g", amplitude_v=1.0, waveform="table",
+                          table_t_us=[0.0], table_v=[1.0])], ok),
+    ]
+
+
+def field_cases():
+    """tracer3d.build_field_aware_3d (float32 and float64 potentials, Python
+    and numpy float64 spacings, with and without the metal rule) and
+    build_stl3d.compose_drive_channels on stand-in specs."""
+    from types import SimpleNamespace
+    from ion_gym.physics.tracer3d import build_field_aware_3d
+    from ion_gym.physics.build_stl3d import compose_drive_channels
+    rng = np.random.default_rng(4242)
+    out = {}
+    grads = [((13, 11, 9), np.float32, 0.1, True),
+             ((13, 11, 9), np.float32, np.float64(0.05), True),
+             ((13, 11, 9), np.float32, 0.3, False),
+             ((10, 7, 12), np.float64, 0.25, True),
+             ((2, 3, 4), np.float32, 0.7, True),
+             ((2, 2, 2), np.float32, np.float64(1.3), True),
+             ((5, 9, 2), np.float32, 1, True)]
+    for idx, (shape, dt, h, aware) in enumerate(grads):
+        phi = _smooth(rng, shape, 40.0).astype(dt)
+        boxes = [((0, 0, 0), (max(1, shape[0] // 3), shape[1], 1)),
+                 ((shape[0] // 2, 1, shape[2] // 2),
+                  (shape[0], max(2, shape[1] // 2), shape[2]))]
+        ele = _labels(rng, shape, boxes)
+        if idx == 3:
+            ele = (ele * 3).astype(np.uint8)
+        ex, ey, ez = build_field_aware_3d(phi, ele, h, electrode_aware=aware)
+        k = f"grad/{idx}"
+        out[k + "/phi"] = phi
+        out[k + "/ele"] = ele
+        out[k + "/h"] = np.array(float(h))
+        out[k + "/h_is_f64"] = np.array(isinstance(h, np.float64))
+        out[k + "/aware"] = np.array(aware)
+        out[k + "/ex"], out[k + "/ey"], out[k + "/ez"] = ex, ey, ez
+    for name, gkw, groups, els in field_specs():
+        shape = (12, 10, 9)
+        bases = {i: np.abs(_smooth(rng, shape, 0.4)) for i in
+                 range(1, len(els) + 1)}
+        ele = _labels(rng, shape, [((0, 0, 0), (3, 10, 2)),
+                                   ((8, 3, 4), (12, 7, 9))])
+        geom = SimpleNamespace(rf_groups=groups, electrodes=els, **gkw)
+        ch = compose_drive_channels(_Spec(geom), bases, ele)
+        k = f"compose/{name}"
+        out[k + "/bases"] = np.stack([bases[i] for i in sorted(bases)])
+        out[k + "/ele"] = ele
+        for key, v in ch.items():
+            if key == "chan_phi":
+                out[k + "/chan_phi"] = (np.stack(v) if v else
+                                        np.zeros((0,) + shape, np.float32))
+            elif key == "ch_name":
+                out[k + "/ch_name"] = np.array(v, dtype=str)
+            else:
+                out[k + "/" + key] = np.asarray(v)
+    shape = (6, 5, 4)
+    bases = {1: _smooth(rng, shape), 2: _smooth(rng, shape)}
+    ele = np.zeros(shape, np.int16)
+    for name, groups, els in field_error_specs():
+        geom = SimpleNamespace(rf_groups=groups, electrodes=els, mm_per_gu=0.1)
+        try:
+            compose_drive_channels(_Spec(geom), bases, ele)
+            raise AssertionError(f"{name}: no refusal")
+        except ValueError as e:
+            out[f"compose_err/{name}/message"] = np.array(str(e))
+    try:
+        geom = SimpleNamespace(rf_groups=[], electrodes=[_El("e1", [], 1.0)],
+                               mm_per_gu=0.1)
+        compose_drive_channels(_Spec(geom), bases, np.zeros((6, 5, 3)))
+        raise AssertionError("shape: no refusal")
+    except ValueError as e:
+        out["compose_err/shape/message"] = np.array(str(e))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
     ap.add_argument("--only", choices=["kernels", "drivers", "theta", "cache",
-                                       "raster"],
+                                       "raster", "field"],
                     default=None)
     a = ap.parse_args()
     import ion_gym.physics.solver3d as S
@@ -473,6 +633,9 @@ def main():
         np.savez_compressed(os.path.join(a.out, "raster.npz"),
                             **raster_cases())
         print("raster.npz written")
+    if a.only in (None, "field"):
+        np.savez_compressed(os.path.join(a.out, "field.npz"), **field_cases())
+        print("field.npz written")
 
 
 if __name__ == "__main__":

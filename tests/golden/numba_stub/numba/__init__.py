@@ -12,6 +12,11 @@ compiled reference computes.  Wrapping each literal in ``np.float64`` /
 float32 op float32 stays float32, anything with a float64 or int64 operand is
 float64.
 
+Arguments are typed the same way: numba types a Python ``float`` argument
+as float64 and a Python ``int`` as int64, so the wrapper passes them on as
+``np.float64`` / ``np.int64`` (``(a_f32 - b_f32) / h`` with ``h`` a Python
+float divides in float64 when compiled).
+
 ``prange`` is ``range``: within one red-black colour the updates are
 independent and the row maxima are order-free, so serial execution gives the
 same bits as numba's parallel execution.
@@ -54,8 +59,23 @@ def _interpret(fn):
     g["__stub_i64"] = np.int64
     ns = {}
     exec(code, g, ns)
-    out = ns[fn.__name__]
+    inner = ns[fn.__name__]
+
+    def _arg(v):
+        if isinstance(v, (bool, np.generic, np.ndarray)):
+            return v
+        if isinstance(v, float):
+            return np.float64(v)
+        if isinstance(v, int):
+            return np.int64(v)
+        return v
+
+    def out(*args, **kwargs):
+        return inner(*[_arg(v) for v in args],
+                     **{k: _arg(v) for k, v in kwargs.items()})
+    out.__name__ = fn.__name__
     out.__wrapped_source__ = src
+    out.__interpreted__ = inner
     return out
 
 
