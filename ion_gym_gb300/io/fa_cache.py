@@ -198,3 +198,94 @@ def load_bases(spec_or_key, root=None):
              if k.startswith("basis_")}
     lab = arrs["labels"]
     return bases, {i: (lab == i) for i in bases}
+
+
+def annotate(spec_or_key, name, label=None, root=None, spec_json=None):
+    """Record which named spec produced or resolved an entry in its
+    provenance.json sidecar (fa_cache.py:219-272): a list of {name, label,
+    when[, spec_json]} records; a repeated (name, label) refreshes its time
+    (and spec_json).  Descriptive only: an unreadable sidecar is rebuilt
+    and a write failure is reported, never raised."""
+    import time
+    key = (spec_or_key if isinstance(spec_or_key, str) else spec_key(spec_or_key))
+    name = (name or "").strip()
+    if not name:
+        return
+    dest = os.path.join(os.path.expanduser(_root(root)), key)
+    if not os.path.isdir(dest):
+        return
+    ppath = os.path.join(dest, "provenance.json")
+    recs = []
+    if os.path.exists(ppath):
+        try:
+            with open(ppath, encoding="utf-8") as f:
+                recs = json.load(f)
+            if not isinstance(recs, list):
+                raise ValueError(f"expected a list, got {type(recs).__name__}")
+        except (OSError, ValueError) as e:
+            print(f"fa_cache: provenance sidecar unreadable for {key} "
+                  f"({e}) — rebuilding it (descriptive data only).")
+            recs = []
+    now = time.strftime("%Y-%m-%d %H:%M")
+    for r in recs:
+        if r.get("name") == name and r.get("label") == label:
+            r["when"] = now
+            if spec_json is not None:
+                r["spec_json"] = spec_json
+            break
+    else:
+        rec = dict(name=name, label=label, when=now)
+        if spec_json is not None:
+            rec["spec_json"] = spec_json
+        recs.append(rec)
+    try:
+        fd, tmp = tempfile.mkstemp(dir=dest, prefix=".prov.")
+        with os.fdopen(fd, "w") as f:
+            json.dump(recs, f, indent=1)
+        os.replace(tmp, ppath)
+    except OSError as e:
+        print(f"fa_cache: could not write provenance for {key} ({e})")
+
+
+def entries(root=None):
+    """[{key, arrays, spec_name, shape, produced_by, has_spec_json}] of the
+    complete-or-not entries under root (fa_cache.py:275-330, the fields a
+    field export needs)."""
+    root = os.path.expanduser(_root(root))
+    out = []
+    if not os.path.isdir(root):
+        return out
+    for name in sorted(os.listdir(root)):
+        p = os.path.join(root, name)
+        if not os.path.isdir(p) or name.startswith("."):
+            continue
+        rec = dict(key=name, arrays=sum(f.endswith(".npy") for f in os.listdir(p)),
+                   spec_name=None, shape=None, produced_by=[], has_spec_json=False,
+                   problems=[])
+        ppath = os.path.join(p, "provenance.json")
+        if os.path.exists(ppath):
+            try:
+                with open(ppath, encoding="utf-8") as f:
+                    precs = json.load(f)
+                if isinstance(precs, list):
+                    rec["produced_by"] = [r.get("name") for r in precs
+                                          if isinstance(r, dict) and r.get("name")]
+                    rec["has_spec_json"] = any(isinstance(r, dict) and r.get("spec_json")
+                                               for r in precs)
+            except (OSError, ValueError) as e:
+                rec["problems"].append(
+                    f"provenance.json unreadable ({type(e).__name__}: {e})")
+        mp = os.path.join(p, "meta.json")
+        if os.path.exists(mp):
+            try:
+                with open(mp, encoding="utf-8") as f:
+                    meta = json.load(f)
+                spec = meta.get("spec", {}) or {}
+                rec["spec_name"] = spec.get("name") if isinstance(spec, dict) else None
+                arrs = meta.get("arrays", {}) or {}
+                if arrs:
+                    rec["shape"] = next(iter(arrs.values())).get("shape")
+            except (OSError, ValueError, KeyError, AttributeError) as e:
+                rec["problems"].append(f"meta.json unreadable ({type(e).__name__}: {e})")
+        out.append(rec)
+    return out

@@ -23,8 +23,13 @@ Fixture files:
   field.npz    tracer3d.build_field_aware_3d and
                build_stl3d.compose_drive_channels on small grids, with the
                messages of the composer's refusals.
+  bundle.npz   io/fa_cache.store + annotate and io/field_io
+               export_field_bundle / import_field_bundle /
+               read_field_arrays on a small 3-D entry: the key, every bundle
+               member, the spec JSON written beside it and the refusals.
 """
 import argparse
+import json
 import os
 import sys
 import time
@@ -603,11 +608,77 @@ def field_cases():
     return out
 
 
+def bundle_spec():
+    """The small 3-D entry of the bundle fixture: (spec, arrays, spec_json)."""
+    rng = np.random.default_rng(99)
+    spec = {"name": "ring deck", "route": "stl3d", "grid": [4, 5, 6],
+            "geometry": {"mm_per_gu": 0.25, "electrodes": [
+                {"name": "e1", "v": 10.0}, {"name": "e2", "v": -3.5}]}}
+    lab = np.zeros((4, 5, 6), np.uint8)
+    lab[0] = 1
+    lab[-1, :, :2] = 2
+    arrays = {"basis_1": rng.random((4, 5, 6)).astype(np.float32),
+              "basis_2": rng.random((4, 5, 6)).astype(np.float32),
+              "labels": lab}
+    spec_json = {"name": "ring deck", "geometry": spec["geometry"]}
+    return spec, arrays, spec_json
+
+
+def bundle_cases():
+    """A cache entry written by the reference, exported as a bundle and
+    imported back under a fresh root."""
+    import tempfile
+    from ion_gym.io import fa_cache
+    from ion_gym.io import field_io
+    out = {}
+    spec, arrays, spec_json = bundle_spec()
+    with tempfile.TemporaryDirectory() as td:
+        root = os.path.join(td, "cache")
+        key = fa_cache.store(spec, arrays, root=root)
+        fa_cache.annotate(key, "ring deck", label="first", root=root,
+                          spec_json=spec_json)
+        npz, deck = field_io.export_field_bundle(key, os.path.join(td, "out"),
+                                                 root=root)
+        out["bundle/0/key"] = np.array(key)
+        out["bundle/0/npz_name"] = np.array(os.path.basename(npz))
+        out["bundle/0/deck_name"] = np.array(os.path.basename(deck))
+        with open(deck, encoding="utf-8") as f:
+            out["bundle/0/deck_text"] = np.array(f.read())
+        with np.load(npz) as z:
+            out["bundle/0/members"] = np.array(sorted(z.files))
+            for m in z.files:
+                out[f"member/{m}/value"] = z[m]
+        bases, labels, meta = field_io.read_field_arrays(npz)
+        out["bundle/0/read_keys"] = np.array(sorted(bases))
+        for k, b in bases.items():
+            out[f"read/{k}/basis"] = b
+        out["bundle/0/read_labels"] = labels
+        out["bundle/0/meta_json"] = np.array(json.dumps(meta, sort_keys=True))
+        root2 = os.path.join(td, "cache2")
+        k2 = field_io.import_field_bundle(npz, root=root2)
+        out["bundle/0/import_key"] = np.array(k2)
+        files = sorted(os.listdir(os.path.join(root2, k2)))
+        out["bundle/0/import_files"] = np.array(files)
+        with open(os.path.join(root2, k2, "meta.json"), "rb") as f:
+            out["bundle/0/import_meta_bytes"] = np.frombuffer(f.read(), np.uint8)
+        bad = dict(spec_json, geometry=dict(spec_json["geometry"], mm_per_gu=0.5))
+
+        class _S:
+            def to_dict(self):
+                return bad
+        try:
+            field_io.import_field_bundle(npz, spec=_S(), root=root2)
+            raise AssertionError("no refusal")
+        except ValueError as e:
+            out["bundle_err/geometry/message"] = np.array(str(e))
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
     ap.add_argument("--only", choices=["kernels", "drivers", "theta", "cache",
-                                       "raster", "field"],
+                                       "raster", "field", "bundle"],
                     default=None)
     a = ap.parse_args()
     import ion_gym.physics.solver3d as S
@@ -636,6 +707,9 @@ def main():
     if a.only in (None, "field"):
         np.savez_compressed(os.path.join(a.out, "field.npz"), **field_cases())
         print("field.npz written")
+    if a.only in (None, "bundle"):
+        np.savez_compressed(os.path.join(a.out, "bundle.npz"), **bundle_cases())
+        print("bundle.npz written")
 
 
 if __name__ == "__main__":
