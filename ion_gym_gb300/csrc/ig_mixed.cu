@@ -524,27 +524,42 @@ k_cg_dir(float* __restrict__ p, const float* __restrict__ z,
   p[o] = z[o] + b * p[o];
 }
 
+// Compensated float32 accumulation (Kahan): a thread sums many products
+// with about float64 accuracy at float32 cost; the block total is formed in
+// float64 once per block.
+struct KSum {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float v) {
+    const float y = __fsub_rn(v, c);
+    const float t = __fadd_rn(s, y);
+    c = __fsub_rn(__fsub_rn(t, s), y);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
 // q = L p (both colours; q = 0 on metal) and block partials of <p, q> and
-// <p, g>; blockIdx.z = colour.
+// <p, g>; blockIdx.z = colour.  Grid-stride over float4 groups (kCgBlocks
+// blocks per colour and problem), so each block reduces once.
+constexpr unsigned kCgBlocks = 152 * 2;
 __global__ void __launch_bounds__(kT)
 k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
             const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ q,
             double* __restrict__ part, size_t pstride) {
   __shared__ double sh[kT / 32];
   const int c = blockIdx.z;
-  const uint32_t t = blockIdx.x * kT + threadIdx.x;
   const uint32_t nq = G.csz >> 2;
-  float spq = 0.f, spg = 0.f;
-  if (t < nq) {
+  KSum spq, spg;
+  const float* pb = p + blockIdx.y * pstride;
+  const float* own = pb + (size_t)c * G.csz;
+  const float* oth = pb + (size_t)(1 - c) * G.csz;
+  for (uint32_t t = blockIdx.x * kT + threadIdx.x; t < nq; t += gridDim.x * kT) {
     const uint32_t ij = fdivu(t, G.dH4);
     const int m0 = 4 * (int)(t - ij * G.dH4.d);
     const int i = (int)fdivu(ij, G.dny);
     const int j = (int)(ij - (uint32_t)i * G.dny.d);
     const int pc = (i + j + c) & 1;
     const uint32_t base = ij * (uint32_t)G.H + m0;
-    const float* pb = p + blockIdx.y * pstride;
-    const float* own = pb + (size_t)c * G.csz;
-    const float* oth = pb + (size_t)(1 - c) * G.csz;
     const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + (size_t)c * G.csz + base);
     const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
     const float4 pv = ld4(own + base);
@@ -558,15 +573,15 @@ k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
       out[u] = 0.f;
       if (!mv[u] && k < G.nz)
         out[u] = 6.0f * pp[u] - nbr_sum(G, own, oth, i, j, m0 + u, k, base + u);
-      spq += pp[u] * out[u];
-      spg += pp[u] * gg[u];
+      spq.add(pp[u] * out[u]);
+      spg.add(pp[u] * gg[u]);
     }
     *reinterpret_cast<float4*>(q + blockIdx.y * pstride + (size_t)c * G.csz + base) =
         make_float4(out[0], out[1], out[2], out[3]);
   }
-  const double a = block_sum_d((double)spq, sh);
+  const double a = block_sum_d(spq.value(), sh);
   __syncthreads();
-  const double b = block_sum_d((double)spg, sh);
+  const double b = block_sum_d(spg.value(), sh);
   if (threadIdx.x == 0) {
     const size_t slot = ((size_t)blockIdx.y * 2 + c) * gridDim.x + blockIdx.x;
     part[2 * slot] = a;
@@ -574,18 +589,23 @@ k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
   }
 }
 
-// block partials of <z, q>
+// block partials of <z, q>: grid-stride over float4 groups, kCgBlocks
+// blocks per problem
 __global__ void __launch_bounds__(kT)
 k_cg_dot(const float* __restrict__ z, const float* __restrict__ q,
          double* __restrict__ part, size_t pstride, uint32_t n) {
   __shared__ double sh[kT / 32];
-  const uint32_t t = blockIdx.x * kT + threadIdx.x;
-  float s = 0.f;
-  if (t < n) {
-    const size_t o = blockIdx.y * pstride + t;
-    s = z[o] * q[o];
+  KSum s;
+  const float* zb = z + blockIdx.y * pstride;
+  const float* qb = q + blockIdx.y * pstride;
+  for (uint32_t t = blockIdx.x * kT + threadIdx.x; t < n / 4; t += gridDim.x * kT) {
+    const float4 a = ld4(zb + 4 * (size_t)t), b = ld4(qb + 4 * (size_t)t);
+    s.add(a.x * b.x);
+    s.add(a.y * b.y);
+    s.add(a.z * b.z);
+    s.add(a.w * b.w);
   }
-  const double a = block_sum_d((double)s, sh);
+  const double a = block_sum_d(s.value(), sh);
   if (threadIdx.x == 0) part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = a;
 }
 
@@ -863,12 +883,13 @@ struct Session {
     MLevel& f = lv[0];
     const uint32_t n = (uint32_t)f.pstride;
     const dim3 gv(nblk(n), B);
-    const unsigned nb4 = nblk(f.G.csz / 4);
+    const unsigned nb4 = std::min(nblk(f.G.csz / 4), kCgBlocks);
+    const unsigned nbd = std::min(nblk(n / 4), kCgBlocks);
     for (int it = 0; it < cg_iters; it++) {
       MK(cudaMemsetAsync(f.e.p, 0, f.pstride * B * 4, s));
       vcycle(0);  // z = f.e
-      k_cg_dot<<<gv, kT, 0, s>>>(f.e.p, qb.p, part.p, f.pstride, n);
-      k_cg_reduce<<<B, kT, 0, s>>>(part.p, (int)nblk(n), 1, scal.p, 1);
+      k_cg_dot<<<dim3(nbd, B), kT, 0, s>>>(f.e.p, qb.p, part.p, f.pstride, n);
+      k_cg_reduce<<<B, kT, 0, s>>>(part.p, (int)nbd, 1, scal.p, 1);
       k_cg_dir<<<gv, kT, 0, s>>>(pb.p, f.e.p, scal.p, f.pstride, n);
       k_cg_matvec<<<dim3(nb4, B, 2), kT, 0, s>>>(pb.p, f.g.p, f.mask.p, f.G, qb.p, part.p,
                                                 f.pstride);
