@@ -313,38 +313,63 @@ __device__ __forceinline__ float cget(const float* eb, const SGeo& C, int i, int
 // e_fine += trilinear(e_coarse) at free fine nodes.  Each axis weight is 0,
 // 1/2 or 1 (fine node i sits at i/2 in coarse units), so a fine node reads
 // only the 1, 2, 4 or 8 coarse values whose weight is nonzero.
+// Over the split layout: thread = 4 consecutive slots
+// of one colour of fine row (i, j) (blockIdx.z = colour), so the 4 nodes
+// share their x/y weights and their k parity (one z pattern for the whole
+// thread) and the fine correction is read and written as one float4.  The
+// per-node sum is formed in x, y, z order.
 __global__ void __launch_bounds__(kT)
-k_prolong_add(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
-              const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
-              size_t fstride) {
+k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
+               const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
+               size_t fstride) {
+  const int c = blockIdx.z;
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
-  if (t >= F.n) return;
-  const uint32_t ij = fdivu(t, F.dnz);
-  const int k = (int)(t - ij * F.dnz.d);
+  if (t >= (F.csz >> 2)) return;
+  const uint32_t ij = fdivu(t, F.dH4);
+  const int m0 = 4 * (int)(t - ij * F.dH4.d);
   const int i = (int)fdivu(ij, F.dny);
   const int j = (int)(ij - (uint32_t)i * F.dny.d);
-  const int c = scol(i, j, k);
-  const uint32_t s = sidx(F, i, j, k);
-  if (maskf[(size_t)c * F.csz + s]) return;
+  const int pc = (i + j + c) & 1;
+  const uint32_t base = ij * (uint32_t)F.H + m0;
+  const uchar4 mk = *reinterpret_cast<const uchar4*>(maskf + (size_t)c * F.csz + base);
+  const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
   const float* eb = ec + blockIdx.y * cstride;
-  const LerpF x = pa(i, C.nx), y = pa(j, C.ny), z = pa(k, C.nz);
-  int xi[2], yi[2], zi[2];
-  float xw[2], yw[2], zw[2];
-  int nxw = 0, nyw = 0, nzw = 0;
+  const LerpF x = pa(i, C.nx), y = pa(j, C.ny);
+  int xi[2], yi[2];
+  float xw[2], yw[2];
+  int nxw = 0, nyw = 0;
   if (x.t != 1.f) { xi[nxw] = x.a0; xw[nxw++] = 1.f - x.t; }
   if (x.t != 0.f) { xi[nxw] = x.a1; xw[nxw++] = x.t; }
   if (y.t != 1.f) { yi[nyw] = y.a0; yw[nyw++] = 1.f - y.t; }
   if (y.t != 0.f) { yi[nyw] = y.a1; yw[nyw++] = y.t; }
-  if (z.t != 1.f) { zi[nzw] = z.a0; zw[nzw++] = 1.f - z.t; }
-  if (z.t != 0.f) { zi[nzw] = z.a1; zw[nzw++] = z.t; }
-  float acc = 0.f;
-  for (int a = 0; a < nxw; a++)
-    for (int b = 0; b < nyw; b++) {
-      float zs = 0.f;
-      for (int q = 0; q < nzw; q++) zs += zw[q] * cget(eb, C, xi[a], yi[b], zi[q]);
-      acc += xw[a] * yw[b] * zs;
-    }
-  ef[fstride * blockIdx.y + (size_t)c * F.csz + s] += acc;
+  float add[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    add[u] = 0.f;
+    const int k = 2 * (m0 + u) + pc;
+    if (mv[u] || k >= F.nz) continue;
+    const LerpF z = pa(k, C.nz);
+    int zi[2];
+    float zw[2];
+    int nzw = 0;
+    if (z.t != 1.f) { zi[nzw] = z.a0; zw[nzw++] = 1.f - z.t; }
+    if (z.t != 0.f) { zi[nzw] = z.a1; zw[nzw++] = z.t; }
+    float acc = 0.f;
+    for (int a = 0; a < nxw; a++)
+      for (int b = 0; b < nyw; b++) {
+        float zs = 0.f;
+        for (int q = 0; q < nzw; q++) zs += zw[q] * cget(eb, C, xi[a], yi[b], zi[q]);
+        acc += xw[a] * yw[b] * zs;
+      }
+    add[u] = acc;
+  }
+  float4* out = reinterpret_cast<float4*>(ef + fstride * blockIdx.y + (size_t)c * F.csz + base);
+  float4 v = *out;
+  v.x += add[0];
+  v.y += add[1];
+  v.z += add[2];
+  v.w += add[3];
+  *out = v;
 }
 
 // Coarsest level: red-black SOR in shared memory, one CTA per problem, a
@@ -846,7 +871,8 @@ struct Session {
     // bottom is solved directly, so once is enough there)
     const int reps = (l + 2 < lv.size()) ? gamma : 1;
     for (int q = 0; q < reps; q++) vcycle(l + 1);
-    k_prolong_add<<<gn, kT, 0, s>>>(b.e.p, b.G, a.e.p, a.mask.p, a.G, b.pstride, a.pstride);
+    k_prolong_add4<<<dim3(nblk(a.G.csz / 4), B, 2), kT, 0, s>>>(b.e.p, b.G, a.e.p, a.mask.p, a.G,
+                                                            b.pstride, a.pstride);
     // post-smoothing in the reverse colour order keeps the cycle symmetric
     for (int q = 0; q < nu2; q++)
       for (int c = 1; c >= 0; c--)
