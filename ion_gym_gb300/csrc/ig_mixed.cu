@@ -33,6 +33,9 @@
 #include <limits>
 #include <string>
 #include <vector>
+#include <array>
+#include <map>
+#include <mutex>
 
 #include "ig_common.cuh"
 #include "ig_internal.h"
@@ -105,35 +108,24 @@ __device__ __forceinline__ float nbr_sum(const SGeo& g, const float* __restrict_
 
 // ---- FP32 kernels on split arrays (blockIdx.y = problem) ----------------
 
-// Four consecutive slots m0..m0+3 of one colour row per thread, 16-byte
-// loads of the neighbour rows (the split layout makes the x/y neighbours of
-// slot m the slots m of the adjacent rows, and the z neighbours slots m-1+p
-// and m+p of the other colour's own row).  Threads whose slots touch a face
-// in z, or grids with a size-1 axis, take the per-slot path.
 __device__ __forceinline__ float4 ld4(const float* p) {
   return *reinterpret_cast<const float4*>(p);
 }
 
-__global__ void __launch_bounds__(kT)
-k_gs4(float* __restrict__ e, const float* __restrict__ g,
-      const uint8_t* __restrict__ mask, SGeo G, int c, float omega,
-      size_t pstride) {
-  const uint32_t t = blockIdx.x * kT + threadIdx.x;
-  const uint32_t nq = G.csz >> 2;
-  if (t >= nq) return;
+// One float4 group (slots m0..m0+3 of colour c, row ij) of the update.
+__device__ __forceinline__ void gs4_group(float* __restrict__ own, const float* __restrict__ oth,
+                                          const float* __restrict__ gp,
+                                          const uint8_t* __restrict__ mp, const SGeo& G,
+                                          int c, float omega, uint32_t t) {
   const uint32_t ij = fdivu(t, G.dH4);
   const int m0 = 4 * (int)(t - ij * G.dH4.d);
   const int i = (int)fdivu(ij, G.dny);
   const int j = (int)(ij - (uint32_t)i * G.dny.d);
   const int p = (i + j + c) & 1;
-  const uint32_t row = ij * (uint32_t)G.H;
-  const uint32_t base = row + m0;
-  const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + (size_t)c * G.csz + base);
+  const uint32_t base = ij * (uint32_t)G.H + m0;
+  const uchar4 mk = *reinterpret_cast<const uchar4*>(mp + base);
   if (mk.x & mk.y & mk.z & mk.w) return;  // all metal or unused slots
-  float* eb = e + blockIdx.y * pstride;
-  float* own = eb + (size_t)c * G.csz;
-  const float* oth = eb + (size_t)(1 - c) * G.csz;
-  const float4 gg = ld4(g + blockIdx.y * pstride + (size_t)c * G.csz + base);
+  const float4 gg = ld4(gp + base);
   const int kmax = 2 * (m0 + 3) + p;
   float q[4];
   const bool fast = G.nx > 1 && G.ny > 1 && G.nz > 1 && m0 >= 1 && kmax <= G.nz - 2;
@@ -163,11 +155,43 @@ k_gs4(float* __restrict__ e, const float* __restrict__ g,
   }
   const float gv[4] = {gg.x, gg.y, gg.z, gg.w};
   const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
+  if (omega == 1.0f && (mk.x | mk.y | mk.z | mk.w) == 0) {
+    *reinterpret_cast<float4*>(own + base) =
+        make_float4((q[0] - gv[0]) * (1.0f / 6.0f), (q[1] - gv[1]) * (1.0f / 6.0f),
+                    (q[2] - gv[2]) * (1.0f / 6.0f), (q[3] - gv[3]) * (1.0f / 6.0f));
+    return;
+  }
 #pragma unroll
   for (int u = 0; u < 4; u++) {
     if (mv[u]) continue;
     const float nv = (q[u] - gv[u]) * (1.0f / 6.0f);
     own[base + u] = omega == 1.0f ? nv : own[base + u] + omega * (nv - own[base + u]);
+  }
+}
+
+// Red-black Gauss-Seidel half-sweep of colour c on the split layout.  Each
+// thread updates NG float4 groups (four consecutive slots of one colour
+// row; 16-byte loads of the neighbour rows -- the split layout makes the
+// x/y neighbours of slot m the slots m of the adjacent rows, and the z
+// neighbours slots m-1+p and m+p of the other colour's own row), the groups
+// blockDim apart so every load instruction stays coalesced.  Groups that
+// touch a face in z, or grids with a size-1 axis, take the per-slot path.
+// NG and the block size are chosen per grid by the session's tuner.
+template <int NG>
+__global__ void k_gs4(float* __restrict__ e, const float* __restrict__ g,
+                      const uint8_t* __restrict__ mask, SGeo G, int c, float omega,
+                      size_t pstride) {
+  const uint32_t nq = G.csz >> 2;
+  float* eb = e + blockIdx.y * pstride;
+  float* own = eb + (size_t)c * G.csz;
+  const float* oth = eb + (size_t)(1 - c) * G.csz;
+  const float* gp = g + blockIdx.y * pstride + (size_t)c * G.csz;
+  const uint8_t* mp = mask + (size_t)c * G.csz;
+  const uint32_t t0 = blockIdx.x * blockDim.x * NG + threadIdx.x;
+#pragma unroll
+  for (int u = 0; u < NG; u++) {
+    const uint32_t t = t0 + u * blockDim.x;
+    if (t < nq) gs4_group(own, oth, gp, mp, G, c, omega, t);
   }
 }
 
@@ -754,6 +778,15 @@ size_t session_bytes(Dims fine, int bmax) {
   return b + 8 * (size_t)bmax;
 }
 
+// Kernel launches the mixed path issued (graph replays count every node).
+std::atomic<long> g_mixed_launches{0};
+
+// Launch shape of the smoother: float4 groups per thread and block size.
+struct GsCfg {
+  int ng = 1;
+  int threads = 256;
+};
+
 // One geometry resident on the device: the FP32 multigrid hierarchy for up
 // to bmax problems, the FP64 potentials, and one CUDA graph per batch size.
 struct Session {
@@ -780,6 +813,8 @@ struct Session {
   double resid_scale = 1.0;
   float bottom_omega = 1.f;
   std::vector<std::pair<int, cudaGraphExec_t>> graphs;
+  GsCfg gs_cfg;          // smoother launch shape, from the tuner
+  bool gs_tuned = false;
 
   ~Session() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
@@ -845,6 +880,76 @@ struct Session {
     MK(cudaGetLastError());
   }
 
+  // One colour half-sweep of level a for nb problems with the tuned shape.
+  void launch_gs(MLevel& a, int c, int nb, float omega) {
+    const uint32_t nq = a.G.csz / 4;
+    const unsigned per = (unsigned)(gs_cfg.threads * gs_cfg.ng);
+    const dim3 grid((nq + per - 1) / per, nb);
+    switch (gs_cfg.ng) {
+      case 4:
+        k_gs4<4><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega, a.pstride);
+        break;
+      case 2:
+        k_gs4<2><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega, a.pstride);
+        break;
+      default:
+        k_gs4<1><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega, a.pstride);
+        break;
+    }
+  }
+
+  // The smoother's launch shape (groups per thread x block size), timed on
+  // this grid's finest level for nb problems: three red-black pairs per
+  // candidate after one warm pair, the fastest kept.  Shapes are cached per
+  // (grid, problem count) for the process.  Runs before the first graph
+  // capture; the level-0 correction it scribbles on is zeroed before use.
+  void tune_gs(int nb) {
+    static std::mutex mu;
+    static std::map<std::array<long, 4>, GsCfg> cache;
+    const std::array<long, 4> key{d.nx, d.ny, d.nz, (long)nb};
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      auto it = cache.find(key);
+      if (it != cache.end()) {
+        gs_cfg = it->second;
+        gs_tuned = true;
+        return;
+      }
+    }
+    MLevel& f = lv[0];
+    cudaEvent_t e0, e1;
+    MK(cudaEventCreate(&e0));
+    MK(cudaEventCreate(&e1));
+    GsCfg best;
+    float best_ms = 1e30f;
+    long launches = 0;
+    for (int ng : {1, 2, 4})
+      for (int th : {128, 256, 512}) {
+        gs_cfg.ng = ng;
+        gs_cfg.threads = th;
+        for (int c = 0; c < 2; c++) launch_gs(f, c, nb, 1.f);
+        MK(cudaEventRecord(e0, s));
+        for (int q = 0; q < 3; q++)
+          for (int c = 0; c < 2; c++) launch_gs(f, c, nb, 1.f);
+        MK(cudaEventRecord(e1, s));
+        MK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        MK(cudaEventElapsedTime(&ms, e0, e1));
+        launches += 8;
+        if (ms < best_ms) {
+          best_ms = ms;
+          best = gs_cfg;
+        }
+      }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    g_mixed_launches.fetch_add(launches);
+    gs_cfg = best;
+    gs_tuned = true;
+    std::lock_guard<std::mutex> lk(mu);
+    cache[key] = best;
+  }
+
   void vcycle(size_t l) {
     MLevel& a = lv[l];
     const dim3 gs(nblk(a.G.csz), B), gn(nblk(a.G.n), B);
@@ -853,10 +958,8 @@ struct Session {
                                             bottom_pairs, a.pstride);
       return;
     }
-    const dim3 g4(nblk(a.G.csz / 4), B);
     for (int q = 0; q < nu1; q++)
-      for (int c = 0; c < 2; c++)
-        k_gs4<<<g4, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, smooth_omega, a.pstride);
+      for (int c = 0; c < 2; c++) launch_gs(a, c, B, smooth_omega);
     MLevel& b = lv[l + 1];
     if (nu1 > 0 && smooth_omega == 1.f) {
       // Gauss-Seidel ended on colour 1: its residual is zero
@@ -875,8 +978,7 @@ struct Session {
                                                             b.pstride, a.pstride);
     // post-smoothing in the reverse colour order keeps the cycle symmetric
     for (int q = 0; q < nu2; q++)
-      for (int c = 1; c >= 0; c--)
-        k_gs4<<<g4, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, smooth_omega, a.pstride);
+      for (int c = 1; c >= 0; c--) launch_gs(a, c, B, smooth_omega);
   }
 
   // one refinement step: FP64 residual, V-cycles on the correction, update
@@ -934,6 +1036,7 @@ struct Session {
     for (auto& g : graphs)
       if (g.first == B) exec = g.second;
     if (!exec) {
+      if (!gs_tuned) tune_gs(B);
       cudaGraph_t graph;
       MK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       if (method == 1)
@@ -999,7 +1102,6 @@ MixedResult run_mixed(Session& M, double acc, int max_steps) {
   return res;
 }
 
-std::atomic<long> g_mixed_launches{0};
 
 int finish(Session& S, const MixedResult& r, double* phi_out, int* steps_out,
            double* dmax_out) {
@@ -1095,16 +1197,14 @@ int ig_mixed_time_gs(void* handle, int n_problems, int pairs, double* ms_per_lau
   }
   try {
     MLevel& f = S->lv[0];
-    const dim3 gs(nblk(f.G.csz / 4), n_problems);
+    if (!S->gs_tuned) S->tune_gs(n_problems);
     cudaEvent_t e0, e1;
     MK(cudaEventCreate(&e0));
     MK(cudaEventCreate(&e1));
-    for (int c = 0; c < 2; c++)  // warm
-      k_gs4<<<gs, kT, 0, S->s>>>(f.e.p, f.g.p, f.mask.p, f.G, c, 1.f, f.pstride);
+    for (int c = 0; c < 2; c++) S->launch_gs(f, c, n_problems, 1.f);  // warm
     MK(cudaEventRecord(e0, S->s));
     for (int q = 0; q < pairs; q++)
-      for (int c = 0; c < 2; c++)
-        k_gs4<<<gs, kT, 0, S->s>>>(f.e.p, f.g.p, f.mask.p, f.G, c, 1.f, f.pstride);
+      for (int c = 0; c < 2; c++) S->launch_gs(f, c, n_problems, 1.f);
     MK(cudaEventRecord(e1, S->s));
     MK(cudaEventSynchronize(e1));
     float ms = 0.f;
