@@ -238,6 +238,34 @@ int ig_theta_scene(const double *table, int n_prims, const uint8_t *metal,
                    long nx, long ny, long nz, int mirror_bits, int iters,
                    float *theta_out);
 
+/* ---- extruded 2-D shapes (build_shapes3d.py:71-243, raster2d.py:113-230)
+ * ig_shape_xsection: one shape's cross-section on in-plane node
+ * coordinates a (na) x b (nb) -> out (na, nb) uint8, float64 throughout.
+ * type 0 rect, params = cx, cy, cos, sin (of -rotation), x0-T, x0+w+T,
+ * y0-T, y0+h+T, rotated (0/1); type 1 ellipse, params = cx, cy, rx+T, ry+T;
+ * type 2 polygon (closed solid: even-odd interior or within sqrt(tol2) of
+ * an edge), params = tol2, poly = 7 rows of n_points: x0, y0, x1, y1,
+ * ex, ey, seg2 (edge j from point j to j+1, wrapping).
+ * ig_shapes_label: the 3-D assembly.  table: 7 long longs per shape, in
+ * electrode order: electrode slot, extrusion axis (0..2; in-plane axes
+ * the next two cyclically), cutout (0/1), offset of its cross-section in
+ * xs (n_a1 x n_a2 bytes), offset of its range in rng (one byte per node
+ * of the axis), n_a1, n_a2.  Per node: additive shapes OR their volume
+ * into the electrode, cutouts AND NOT theirs; labels_out = the last
+ * electrode (electrode_index[slot]) claiming the node, 0 vacuum; per slot
+ * the node count, the count of nodes already claimed by an earlier
+ * electrode and the lowest such flat index. */
+int ig_shape_xsection(int type, const double *params, int n_params,
+                      const double *poly, int n_points, const double *a,
+                      long na, const double *b, long nb, uint8_t *out);
+int ig_shapes_label(const long long *table, int n_shapes, const uint8_t *xs,
+                    long long xs_len, const uint8_t *rng, long long rng_len,
+                    const int *electrode_index, int n_electrodes, long nx,
+                    long ny, long nz, int16_t *labels_out,
+                    unsigned long long *counts_out,
+                    unsigned long long *clash_counts_out,
+                    unsigned long long *clash_first_out);
+
 /* ---- fields from solved bases ------------------------------------------ *
  * Unit bases, drive superposition and the electrode-aware E-field, the same
  * bits as the reference.

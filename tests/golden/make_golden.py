@@ -23,6 +23,9 @@ Fixture files:
   field.npz    tracer3d.build_field_aware_3d and
                build_stl3d.compose_drive_channels on small grids, with the
                messages of the composer's refusals.
+  shapes.npz   physics/build_shapes3d.shapes_masks_3d on decks of rotated
+               rects, ellipses, polygons and cutouts extruded along x, y and
+               z (origin, mirror), as label grids, and its refusals.
   bundle.npz   io/fa_cache.store + annotate and io/field_io
                export_field_bundle / import_field_bundle /
                read_field_arrays on a small 3-D entry: the key, every bundle
@@ -608,6 +611,132 @@ def field_cases():
     return out
 
 
+def _deck(electrodes, width=4.0, height=3.0, depth=3.0, pitch=0.25,
+          mirror=None, origin=None):
+    g = {"width_mm": width, "height_mm": height, "depth_mm": depth,
+         "mm_per_gu": pitch,
+         "symmetry": {"coords": "xyz", "planes": mirror or {}},
+         "electrodes": electrodes}
+    if origin is not None:
+        g["origin_mm"] = origin
+    return {"name": "shapes_deck",
+            "source": {"seed": 0, "distribution": "disc", "n_ions": 100,
+                       "x0_mm": 1.0, "y0_mm": 0.0, "z0_mm": 0.0, "r_mm": 4.0,
+                       "ke_lo": 0.1, "ke_hi": 1.9, "mz_list": [556.0],
+                       "tob_span_us": 2.0},
+            "integration": {"dt_ns": 1.0, "t_max_us": 400.0},
+            "geometry": g}
+
+
+def shapes_decks():
+    """(name, deck dict) of the shapes fixture: labelled decks first, then
+    the refusals."""
+    ez = {"axis": "z", "lo_mm": 0.5, "hi_mm": 1.0}
+    tri = [[1.9, 1.8], [2.4, 2.3], [1.7, 2.6]]
+    ok = [
+        ("mixed", _deck([
+            {"name": "E1", "shapes": [{"type": "rect", "x_mm": 1.0, "y_mm": 0.5,
+                                       "width_mm": 2.0, "height_mm": 1.5,
+                                       "extrude": ez}]},
+            {"name": "E2", "shapes": [
+                {"type": "ellipse", "cx_mm": 2.0, "cy_mm": 2.2, "rx_mm": 1.1,
+                 "ry_mm": 0.55,
+                 "extrude": {"axis": "x", "lo_mm": 1.5, "hi_mm": 3.5}},
+                {"type": "cutout", "children": [{"type": "polygon",
+                                                  "points_mm": tri}]}]},
+            {"name": "E3", "shapes": [
+                {"type": "rect", "x_mm": 0.25, "y_mm": 2.0, "width_mm": 1.0,
+                 "height_mm": 0.5, "rotation_deg": 30.0,
+                 "extrude": {"axis": "y", "lo_mm": 2.25, "hi_mm": 3.0}},
+                {"type": "polygon", "points_mm": [[0.0, 0.0], [0.75, 0.0],
+                                                  [0.75, 0.5], [0.25, 1.0]]}]},
+        ])),
+        ("origin", _deck([
+            {"name": "A", "shapes": [{"type": "rect", "x_mm": -1.0, "y_mm": -0.5,
+                                      "width_mm": 1.5, "height_mm": 1.0}]},
+            {"name": "B", "shapes": [{"type": "ellipse", "cx_mm": 1.5,
+                                      "cy_mm": 0.75, "rx_mm": 0.6, "ry_mm": 0.9,
+                                      "extrude": {"axis": "z", "lo_mm": 1.0,
+                                                  "hi_mm": 2.5}}]},
+        ], origin=[-1.5, -1.0])),
+        ("mirror", _deck([
+            {"name": "M", "shapes": [{"type": "polygon",
+                                      "points_mm": [[0.5, 0.5], [3.0, 0.75],
+                                                    [2.0, 2.5]],
+                                      "extrude": {"axis": "z", "lo_mm": 0.0,
+                                                  "hi_mm": 0.5}}]},
+        ], mirror={"z": "mirror"})),
+    ]
+    bad = [
+        ("empty", _deck([
+            {"name": "A", "shapes": [{"type": "rect", "x_mm": 1.0, "y_mm": 1.0,
+                                      "width_mm": 1.0, "height_mm": 1.0}]},
+            {"name": "tiny", "shapes": [
+                {"type": "rect", "x_mm": 3.0, "y_mm": 2.0, "width_mm": 0.5,
+                 "height_mm": 0.5},
+                {"type": "cutout", "children": [{"type": "rect", "x_mm": 2.9,
+                                                  "y_mm": 1.9, "width_mm": 0.7,
+                                                  "height_mm": 0.7}]}]}])),
+        ("clash", _deck([
+            {"name": "A", "shapes": [{"type": "rect", "x_mm": 1.0, "y_mm": 1.0,
+                                      "width_mm": 1.0, "height_mm": 1.0}]},
+            {"name": "B", "shapes": [{"type": "ellipse", "cx_mm": 2.0,
+                                      "cy_mm": 1.5, "rx_mm": 0.5,
+                                      "ry_mm": 0.5}]}])),
+        ("zero_shape", _deck([
+            {"name": "A", "shapes": [
+                {"type": "rect", "x_mm": 1.0, "y_mm": 1.0, "width_mm": 1.0,
+                 "height_mm": 1.0},
+                {"type": "rect", "x_mm": 1.01, "y_mm": 1.01, "width_mm": 0.1,
+                 "height_mm": 0.1}]}])),
+        ("zero_cutout", _deck([
+            {"name": "A", "shapes": [
+                {"type": "rect", "x_mm": 1.0, "y_mm": 1.0, "width_mm": 1.0,
+                 "height_mm": 1.0},
+                {"type": "cutout", "children": [{"type": "ellipse",
+                                                  "cx_mm": 3.1, "cy_mm": 0.1,
+                                                  "rx_mm": 0.05,
+                                                  "ry_mm": 0.05}]}]}])),
+        ("outside", _deck([
+            {"name": "A", "shapes": [{"type": "rect", "x_mm": 1.0, "y_mm": 1.0,
+                                      "width_mm": 1.0, "height_mm": 1.0,
+                                      "extrude": {"axis": "z", "lo_mm": 5.0,
+                                                  "hi_mm": 6.0}}]}])),
+        ("mirror_lo", _deck([
+            {"name": "A", "shapes": [{"type": "rect", "x_mm": 1.0, "y_mm": 1.0,
+                                      "width_mm": 1.0, "height_mm": 1.0,
+                                      "extrude": {"axis": "z", "lo_mm": -0.5,
+                                                  "hi_mm": 1.0}}]}],
+            mirror={"z": "mirror"})),
+        ("no_shapes", _deck([
+            {"name": "A", "shapes": [{"type": "rect", "x_mm": 1.0, "y_mm": 1.0,
+                                      "width_mm": 1.0, "height_mm": 1.0}]},
+            {"name": "B", "shapes": []}])),
+    ]
+    return ok, bad
+
+
+def shapes_cases():
+    from ion_gym.io.sim_spec import SimSpec
+    from ion_gym.physics.build_shapes3d import shapes_masks_3d
+    out = {}
+    ok, bad = shapes_decks()
+    for name, d in ok:
+        masks = shapes_masks_3d(SimSpec.from_dict(d))
+        shape = next(iter(masks.values())).shape
+        lab = np.zeros(shape, np.int16)
+        for i, m in masks.items():
+            lab[m] = i
+        out[f"shapes/{name}/lab"] = lab
+    for name, d in bad:
+        try:
+            shapes_masks_3d(SimSpec.from_dict(d))
+            raise AssertionError(f"{name}: no refusal")
+        except ValueError as e:
+            out[f"shapes_err/{name}/message"] = np.array(str(e))
+    return out
+
+
 def bundle_spec():
     """The small 3-D entry of the bundle fixture: (spec, arrays, spec_json)."""
     rng = np.random.default_rng(99)
@@ -678,7 +807,7 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
     ap.add_argument("--only", choices=["kernels", "drivers", "theta", "cache",
-                                       "raster", "field", "bundle"],
+                                       "raster", "field", "bundle", "shapes"],
                     default=None)
     a = ap.parse_args()
     import ion_gym.physics.solver3d as S
@@ -707,6 +836,9 @@ def main():
     if a.only in (None, "field"):
         np.savez_compressed(os.path.join(a.out, "field.npz"), **field_cases())
         print("field.npz written")
+    if a.only in (None, "shapes"):
+        np.savez_compressed(os.path.join(a.out, "shapes.npz"), **shapes_cases())
+        print("shapes.npz written")
     if a.only in (None, "bundle"):
         np.savez_compressed(os.path.join(a.out, "bundle.npz"), **bundle_cases())
         print("bundle.npz written")
