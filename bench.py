@@ -274,6 +274,27 @@ def run_ours(a):
                      if peak else None},
         "clocks": ck,
     }
+    if rank == 0 and ws == 1:
+        # the same quadrupole through the mixed-precision session (FP32
+        # multigrid inside FP64 refinement) to 1e-9 of the 2 V span, host
+        # buffers in and out like e2e, against the FP64 cascadic result
+        from ion_gym_gb300.physics.mixed import MixedSession
+        phi64 = phi_h.numpy().copy()
+        with MixedSession(fixed, 1) as sess:
+            sess.solve_values(val, accuracy=1e-9)
+            torch.cuda.synchronize()
+            tm = time.perf_counter()
+            for _ in range(a.steps):
+                phi_m = sess.solve_values(val, accuracy=1e-9)
+            el_m = time.perf_counter() - tm
+            line["mixed"] = {
+                "value": a.steps / el_m, "unit": "solves/s",
+                "path": "MixedSession.solve_values, host buffers in and out",
+                "accuracy_of_span": 1e-9,
+                "refinement_steps": sess.last_steps,
+                "over_fp64_e2e": (a.steps / el_m) / (a.steps / el_e2e),
+                "max_abs_diff_vs_fp64_cascadic_of_span":
+                    float(np.abs(phi_m[0] - phi64).max()) / 2.0}
     if rank == 0 and ws == 1 and not a.no_cpu:
         g, pairs, secs, thr = cpu_sample(fixed, seconds=a.cpu_seconds)
         line["cpu_baseline"] = {
