@@ -58,7 +58,7 @@ struct SGeo {
                             // up to a multiple of 4 (16-byte aligned rows)
   uint32_t csz;             // nx * ny * H (one colour array)
   uint32_t n;               // nx * ny * nz (natural)
-  FastDiv dH, dny, dnz, dH4;
+  FastDiv dH, dny, dnz, dH4, dH8;  // dH8: pairs of float4 groups per row
 };
 
 SGeo sgeo(const Dims& d) {
@@ -71,6 +71,7 @@ SGeo sgeo(const Dims& d) {
   g.n = (uint32_t)d.n();
   g.dH = FastDiv((uint32_t)g.H);
   g.dH4 = FastDiv((uint32_t)(g.H / 4));
+  g.dH8 = FastDiv((uint32_t)((g.H / 4 + 1) / 2));
   g.dny = FastDiv((uint32_t)d.ny);
   g.dnz = FastDiv((uint32_t)d.nz);
   return g;
@@ -113,14 +114,10 @@ __device__ __forceinline__ float4 ld4(const float* p) {
 }
 
 // One float4 group (slots m0..m0+3 of colour c, row ij) of the update.
-__device__ __forceinline__ void gs4_group(float* __restrict__ own, const float* __restrict__ oth,
-                                          const float* __restrict__ gp,
-                                          const uint8_t* __restrict__ mp, const SGeo& G,
-                                          int c, float omega, uint32_t t) {
-  const uint32_t ij = fdivu(t, G.dH4);
-  const int m0 = 4 * (int)(t - ij * G.dH4.d);
-  const int i = (int)fdivu(ij, G.dny);
-  const int j = (int)(ij - (uint32_t)i * G.dny.d);
+__device__ __forceinline__ void gs4_at(float* __restrict__ own, const float* __restrict__ oth,
+                                       const float* __restrict__ gp,
+                                       const uint8_t* __restrict__ mp, const SGeo& G, int c,
+                                       float omega, uint32_t ij, int i, int j, int m0) {
   const int p = (i + j + c) & 1;
   const uint32_t base = ij * (uint32_t)G.H + m0;
   const uchar4 mk = *reinterpret_cast<const uchar4*>(mp + base);
@@ -169,6 +166,17 @@ __device__ __forceinline__ void gs4_group(float* __restrict__ own, const float* 
   }
 }
 
+__device__ __forceinline__ void gs4_group(float* __restrict__ own, const float* __restrict__ oth,
+                                          const float* __restrict__ gp,
+                                          const uint8_t* __restrict__ mp, const SGeo& G,
+                                          int c, float omega, uint32_t t) {
+  const uint32_t ij = fdivu(t, G.dH4);
+  const int m0 = 4 * (int)(t - ij * G.dH4.d);
+  const int i = (int)fdivu(ij, G.dny);
+  const int j = (int)(ij - (uint32_t)i * G.dny.d);
+  gs4_at(own, oth, gp, mp, G, c, omega, ij, i, j, m0);
+}
+
 // Red-black Gauss-Seidel half-sweep of colour c on the split layout.  Each
 // thread updates NG float4 groups (four consecutive slots of one colour
 // row; 16-byte loads of the neighbour rows -- the split layout makes the
@@ -193,6 +201,30 @@ __global__ void k_gs4(float* __restrict__ e, const float* __restrict__ g,
     const uint32_t t = t0 + u * blockDim.x;
     if (t < nq) gs4_group(own, oth, gp, mp, G, c, omega, t);
   }
+}
+
+// The same half-sweep with two consecutive float4 groups of one row per
+// thread (slots m0..m0+7): one index computation and one mask / z-boundary
+// lookup serve eight slots.  A row with an odd number of groups leaves the
+// second group of its last pair idle.
+__global__ void k_gs8(float* __restrict__ e, const float* __restrict__ g,
+                      const uint8_t* __restrict__ mask, SGeo G, int c, float omega,
+                      size_t pstride) {
+  const uint32_t H4 = (uint32_t)(G.H >> 2);
+  const uint32_t npair = (uint32_t)G.nx * G.ny * G.dH8.d;
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npair) return;
+  const uint32_t ij = fdivu(t, G.dH8);
+  const uint32_t q0 = 2 * (t - ij * G.dH8.d);
+  float* eb = e + blockIdx.y * pstride;
+  float* own = eb + (size_t)c * G.csz;
+  const float* oth = eb + (size_t)(1 - c) * G.csz;
+  const float* gp = g + blockIdx.y * pstride + (size_t)c * G.csz;
+  const uint8_t* mp = mask + (size_t)c * G.csz;
+  const int i = (int)fdivu(ij, G.dny);
+  const int j = (int)(ij - (uint32_t)i * G.dny.d);
+  gs4_at(own, oth, gp, mp, G, c, omega, ij, i, j, 4 * (int)q0);
+  if (q0 + 1 < H4) gs4_at(own, oth, gp, mp, G, c, omega, ij, i, j, 4 * (int)q0 + 4);
 }
 
 // Residual r = g - A e of colour 0 only, in split layout.  After a red-black
@@ -781,7 +813,8 @@ size_t session_bytes(Dims fine, int bmax) {
 // Kernel launches the mixed path issued (graph replays count every node).
 std::atomic<long> g_mixed_launches{0};
 
-// Launch shape of the smoother: float4 groups per thread and block size.
+// Launch shape of the smoother: float4 groups per thread (1, 2, 4 spread a
+// block apart; 8 = k_gs8, two consecutive groups of a row) and block size.
 struct GsCfg {
   int ng = 1;
   int threads = 256;
@@ -885,6 +918,12 @@ struct Session {
     const uint32_t nq = a.G.csz / 4;
     const unsigned per = (unsigned)(gs_cfg.threads * gs_cfg.ng);
     const dim3 grid((nq + per - 1) / per, nb);
+    if (gs_cfg.ng == 8) {
+      const uint32_t npair = (uint32_t)a.G.nx * a.G.ny * a.G.dH8.d;
+      const dim3 g8((npair + gs_cfg.threads - 1) / gs_cfg.threads, nb);
+      k_gs8<<<g8, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega, a.pstride);
+      return;
+    }
     switch (gs_cfg.ng) {
       case 4:
         k_gs4<4><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega, a.pstride);
@@ -923,7 +962,7 @@ struct Session {
     GsCfg best;
     float best_ms = 1e30f;
     long launches = 0;
-    for (int ng : {1, 2, 4})
+    for (int ng : {1, 2, 4, 8})
       for (int th : {128, 256, 512}) {
         gs_cfg.ng = ng;
         gs_cfg.threads = th;
