@@ -366,7 +366,7 @@ def _mixed_launches(L):
 
 
 def run_rings(a):
-    """BASELINE config 3: the 8 unit bases of a seeded ring stack
+    """Batched ring-stack bases: the 8 unit bases of a seeded ring stack
     (193x193x385) in one batch, mixed precision to 1e-9 of the span, against
     the FP64 drop-in (the reference's V-cycle basis door at tol = 1e-9 x
     span, bit-identical to the reference)."""
@@ -467,7 +467,7 @@ def run_rings(a):
 
 
 def run_uneven(a):
-    """BASELINE config 4: 64 seeded geometries, cubic sides from
+    """Uneven batch: 64 seeded geometries, cubic sides from
     {33,65,97,129,193,257}, 2-16 random electrodes at U(-100,100) V, each
     solved to 1e-9 of its span by the mixed path; the geometries run
     concurrently (one resident session and CUDA stream each, `workers`
@@ -509,7 +509,7 @@ def run_uneven(a):
 
 
 def run_serve(a):
-    """BASELINE config 5: Poisson arrivals of basis-solve requests (planar
+    """Served load: Poisson arrivals of basis-solve requests (planar
     boards up to 512x128x96 with 8-32 extruded electrodes on two layers,
     plus the grounded box), continuous batching, resident geometries, HBM
     admission; p50/p99 latency beside throughput."""
