@@ -13,6 +13,7 @@
 // consecutive doubles of a row and every lane does useful FP64 work; the
 // flattened index is split with 32-bit multiplicative division.
 #include <atomic>
+#include <mutex>
 
 #include "ig_common.cuh"
 #include "ig_internal.h"
@@ -281,6 +282,92 @@ k_sweep_rhs(double* __restrict__ e, const uint8_t* __restrict__ fixed,
     }
   }
   block_max_to(mb, dslot);
+}
+
+
+// The bottom of multigrid3d._solve_err (multigrid3d.py:575-580) in one
+// CTA: e = 0; tol = rel_tol * max(max|f|, 1e-300) / 6 (NaN in f makes tol
+// NaN, as numpy's max does); red-black _sweep_rhs pairs at omega until the
+// larger of a pair's two max |update| is below 0.02 * tol, at most
+// max_pairs pairs.  The level lives in shared memory (e, f: 8 B, mask: 1 B
+// per node), every node update is the launched kernel's arithmetic, and the
+// maxima are order-free, so the result and the pair count equal the
+// launched loop's, without a launch or a host synchronisation per pair.
+constexpr int kBottomCta = 1024;
+
+__device__ __forceinline__ unsigned long long cta_max(unsigned long long v,
+                                                      unsigned long long* red) {
+  v = warp_max_u64(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0ull;
+    v = warp_max_u64(v);
+    if (lane == 0) red[32] = v;
+  }
+  __syncthreads();
+  const unsigned long long r = red[32];
+  __syncthreads();
+  return r;
+}
+
+__global__ void __launch_bounds__(kBottomCta)
+k_bottom_err(double* __restrict__ e_out, const uint8_t* __restrict__ fixed_g,
+             const double* __restrict__ f_g, long nx, long ny, long nz, double rel_tol,
+             double omega, long max_pairs) {
+  extern __shared__ double sm[];
+  __shared__ unsigned long long red[33];
+  const long n = nx * ny * nz;
+  double* e = sm;
+  double* f = sm + n;
+  uint8_t* fx = reinterpret_cast<uint8_t*>(sm + 2 * n);
+  unsigned long long fk = 0;
+  bool nan = false;
+  for (long t = threadIdx.x; t < n; t += blockDim.x) {
+    const double v = f_g[t];
+    f[t] = v;
+    fx[t] = fixed_g[t];
+    e[t] = 0.0;
+    const unsigned long long x =
+        static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7fffffffffffffffULL;
+    if (x > 0x7ff0000000000000ULL) nan = true;
+    else if (x > fk) fk = x;
+  }
+  nan = __syncthreads_or(nan);
+  fk = cta_max(fk, red);
+  double scale = nan ? __longlong_as_double(0x7ff8000000000000LL) : bits_to_double(fk);
+  scale = (1e-300 > scale) ? 1e-300 : scale;  // max(|f|.max(), 1e-300)
+  const double tol = __dmul_rn(0.02, __ddiv_rn(__dmul_rn(rel_tol, scale), 6.0));
+  const long half = nz / 2 + 1;  // slots of one colour in a row
+  for (long pr = 0; pr < max_pairs; pr++) {
+    unsigned long long key[2];
+    for (int colour = 0; colour < 2; colour++) {
+      unsigned long long mb = 0;
+      for (long t = threadIdx.x; t < nx * ny * half; t += blockDim.x) {
+        const long ij = t / half, kk = t - ij * half;
+        const long i = ij / ny, j = ij - i * ny;
+        const long k = 2 * kk + ((i + j + colour) & 1);
+        if (k >= nz) continue;
+        const long p = (i * ny + j) * nz + k;
+        if (fx[p]) continue;
+        const Nb nb = neighbours(i, j, k, nx, ny, nz);
+        double v[6];
+        load6(e, nb, v);
+        const double old = e[p];
+        const double nv = div6(__dsub_rn(sum6(v), f[p]));
+        const double nw = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(nv, old)));
+        const unsigned long long x = absbits(__dsub_rn(nw, old));
+        if (x > mb) mb = x;
+        e[p] = nw;
+      }
+      __syncthreads();
+      key[colour] = cta_max(mb, red);
+    }
+    const double d = bits_to_double(key[0] > key[1] ? key[0] : key[1]);
+    if (d < tol) break;
+  }
+  for (long t = threadIdx.x; t < n; t += blockDim.x) e_out[t] = e[t];
 }
 
 // multigrid3d._residual_rhs (multigrid3d.py:394-417).
@@ -633,6 +720,22 @@ void launch_sweep_rhs(cudaStream_t s, double* e, const uint8_t* fixed,
     k_sweep_rhs<true><<<nb, kThreads, 0, s>>>(e, fixed, f, g, omega, colour, dslot, ctl, lp);
   else
     k_sweep_rhs<false><<<nb, kThreads, 0, s>>>(e, fixed, f, g, omega, colour, dslot, ctl, lp);
+}
+
+bool launch_bottom_err(cudaStream_t s, double* e, const uint8_t* fixed, const double* f,
+                       Dims d, double rel_tol, double omega, long max_pairs) {
+  const size_t n = d.n();
+  const size_t bytes = 17 * n;
+  if (n == 0 || bytes > kBottomSmemMax) return false;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_bottom_err, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)kBottomSmemMax);
+  });
+  k_bottom_err<<<1, kBottomCta, (bytes + 7) / 8 * 8, s>>>(e, fixed, f, d.nx, d.ny, d.nz,
+                                                         rel_tol, omega, max_pairs);
+  counted();
+  return true;
 }
 
 void launch_residual_rhs(cudaStream_t s, const double* e, const uint8_t* fixed,

@@ -68,6 +68,13 @@ void launch_sweep(cudaStream_t s, double* phi, const uint8_t* fixed,
 void launch_residual(cudaStream_t s, const double* phi, const uint8_t* fixed,
                      const float* th, int kind, Dims d, double* out,
                      unsigned long long* absmax /* nullable */);
+// The whole bottom solve of multigrid3d._solve_err (e = 0, tol from
+// max|f|, SOR pairs to 0.02 tol, at most max_pairs) in one CTA with the
+// level in shared memory; false (nothing launched) when the level does not
+// fit in kBottomSmemMax bytes (17 per node).
+constexpr size_t kBottomSmemMax = 200 * 1024;
+bool launch_bottom_err(cudaStream_t s, double* e, const uint8_t* fixed, const double* f,
+                       Dims d, double rel_tol, double omega, long max_pairs);
 void launch_sweep_rhs(cudaStream_t s, double* e, const uint8_t* fixed,
                       const double* f, Dims d, double omega, int colour,
                       unsigned long long* dslot, PairCtl* ctl, int lp);

@@ -326,6 +326,11 @@ void build_err_levels(ThreadCtx& c, VCycle& v, const uint8_t* fine_fixed,
 void solve_err(ThreadCtx& c, VCycle& v, size_t L) {
   ErrLevel& a = v.lv[L];
   const size_t n = a.d.n();
+  if (a.bottom && launch_bottom_err(c.s, a.e.p, a.fixed.p, a.f.p, a.d, v.rel_tol,
+                                    v.bottom_omega, 20000)) {
+    CK(cudaGetLastError());
+    return;
+  }
   CK(cudaMemsetAsync(a.e.p, 0, n * 8, c.s));
   const double fmax = device_absmax(c, a.f.p, nullptr, n, v.red);
   const double scale = (1e-300 > fmax) ? 1e-300 : fmax;  // max(|f|.max(), 1e-300)
