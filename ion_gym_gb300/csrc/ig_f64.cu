@@ -285,122 +285,12 @@ k_sweep_rhs(double* __restrict__ e, const uint8_t* __restrict__ fixed,
 }
 
 
-// The bottom of multigrid3d._solve_err (multigrid3d.py:575-580) in one
-// CTA: e = 0; tol = rel_tol * max(max|f|, 1e-300) / 6 (NaN in f makes tol
-// NaN, as numpy's max does); red-black _sweep_rhs pairs at omega until the
-// larger of a pair's two max |update| is below 0.02 * tol, at most
-// max_pairs pairs.  The level lives in shared memory (e, f: 8 B, mask: 1 B
-// per node), every node update is the launched kernel's arithmetic, and the
-// maxima are order-free, so the result and the pair count equal the
-// launched loop's, without a launch or a host synchronisation per pair.
-constexpr int kBottomCta = 1024;
-
-__device__ __forceinline__ unsigned long long cta_max(unsigned long long v,
-                                                      unsigned long long* red) {
-  v = warp_max_u64(v);
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  if (lane == 0) red[wid] = v;
-  __syncthreads();
-  if (wid == 0) {
-    v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0ull;
-    v = warp_max_u64(v);
-    if (lane == 0) red[32] = v;
-  }
-  __syncthreads();
-  const unsigned long long r = red[32];
-  __syncthreads();
-  return r;
-}
-
-__global__ void __launch_bounds__(kBottomCta)
-k_bottom_err(double* __restrict__ e_out, const uint8_t* __restrict__ fixed_g,
-             const double* __restrict__ f_g, long nx, long ny, long nz, double rel_tol,
-             double omega, long max_pairs) {
-  extern __shared__ double sm[];
-  __shared__ unsigned long long red[33];
-  const long n = nx * ny * nz;
-  double* e = sm;
-  double* f = sm + n;
-  uint8_t* fx = reinterpret_cast<uint8_t*>(sm + 2 * n);
-  unsigned long long fk = 0;
-  bool nan = false;
-  for (long t = threadIdx.x; t < n; t += blockDim.x) {
-    const double v = f_g[t];
-    f[t] = v;
-    fx[t] = fixed_g[t];
-    e[t] = 0.0;
-    const unsigned long long x =
-        static_cast<unsigned long long>(__double_as_longlong(v)) & 0x7fffffffffffffffULL;
-    if (x > 0x7ff0000000000000ULL) nan = true;
-    else if (x > fk) fk = x;
-  }
-  nan = __syncthreads_or(nan);
-  fk = cta_max(fk, red);
-  double scale = nan ? __longlong_as_double(0x7ff8000000000000LL) : bits_to_double(fk);
-  scale = (1e-300 > scale) ? 1e-300 : scale;  // max(|f|.max(), 1e-300)
-  const double tol = __dmul_rn(0.02, __ddiv_rn(__dmul_rn(rel_tol, scale), 6.0));
-  const long half = nz / 2 + 1;  // slots of one colour in a row
-  for (long pr = 0; pr < max_pairs; pr++) {
-    unsigned long long key[2];
-    for (int colour = 0; colour < 2; colour++) {
-      unsigned long long mb = 0;
-      for (long t = threadIdx.x; t < nx * ny * half; t += blockDim.x) {
-        const long ij = t / half, kk = t - ij * half;
-        const long i = ij / ny, j = ij - i * ny;
-        const long k = 2 * kk + ((i + j + colour) & 1);
-        if (k >= nz) continue;
-        const long p = (i * ny + j) * nz + k;
-        if (fx[p]) continue;
-        const Nb nb = neighbours(i, j, k, nx, ny, nz);
-        double v[6];
-        load6(e, nb, v);
-        const double old = e[p];
-        const double nv = div6(__dsub_rn(sum6(v), f[p]));
-        const double nw = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(nv, old)));
-        const unsigned long long x = absbits(__dsub_rn(nw, old));
-        if (x > mb) mb = x;
-        e[p] = nw;
-      }
-      __syncthreads();
-      key[colour] = cta_max(mb, red);
-    }
-    const double d = bits_to_double(key[0] > key[1] ? key[0] : key[1]);
-    if (d < tol) break;
-  }
-  for (long t = threadIdx.x; t < n; t += blockDim.x) e_out[t] = e[t];
-}
-
-// multigrid3d._residual_rhs (multigrid3d.py:394-417).
-__global__ void __launch_bounds__(kThreads)
-k_residual_rhs(const double* __restrict__ e, const uint8_t* __restrict__ fixed,
-               const double* __restrict__ f, FlatGeom g,
-               double* __restrict__ out) {
-  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
-  if (t >= g.total) return;
-  const uint32_t ij = fdiv(t, g.div_nz);
-  const uint32_t k = t - ij * g.div_nz.d;
-  const uint32_t i = fdiv(ij, g.div_ny);
-  const uint32_t j = ij - i * g.div_ny.d;
-  double r = 0.0;
-  if (!fixed[t]) {
-    const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
-    double v[6];
-    load6(e, n, v);
-    r = __dsub_rn(__dsub_rn(sum6(v), __dmul_rn(6.0, e[t])), f[t]);
-  }
-  out[t] = r;
-}
-
-// multigrid3d._restrict_fw_njit (multigrid3d.py:420-455).
-__global__ void __launch_bounds__(kThreads)
-k_restrict(const double* __restrict__ fine, long nx, long ny, long nz,
-           double* __restrict__ out, FlatGeom c, int neg4) {
-  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
-  if (t >= c.total) return;
-  const uint32_t ij = fdiv(t, c.div_nz);
-  const long kc = t - ij * c.div_nz.d;
-  const long ic = fdiv(ij, c.div_ny);
-  const long jc = ij - ic * c.div_ny.d;
+// multigrid3d._restrict_fw_njit (multigrid3d.py:420-455) at coarse node
+// (ic, jc, kc): 27-point full weighting with clamped edges, /8, and
+// -4x when neg4 (the caller's scaling).
+__device__ __forceinline__ double restrict_node(const double* __restrict__ fine, long nx,
+                                                long ny, long nz, long ic, long jc, long kc,
+                                                int neg4) {
   const long i = 2 * ic, j = 2 * jc, k = 2 * kc;
   double acc = 0.0;
 #pragma unroll
@@ -426,7 +316,7 @@ k_restrict(const double* __restrict__ fine, long nx, long ny, long nz,
   }
   double r = __dmul_rn(acc, 0.125);  // == acc / 8.0 (power-of-two scale)
   if (neg4) r = -__dmul_rn(r, 4.0);
-  out[t] = r;
+  return r;
 }
 
 struct Lerp {
@@ -476,6 +366,145 @@ __device__ __forceinline__ double trilinear(const double* __restrict__ c,
   const double c0 = lerp_ref(c00, c10, y.t);
   const double c1 = lerp_ref(c01, c11, y.t);
   return lerp_ref(c0, c1, z.t);
+}
+
+// One CTA solving the bottom of multigrid3d._solve_err
+// (multigrid3d.py:575-580) from shared memory: every node update is the
+// launched kernel's arithmetic and the maxima are order-free, so the result
+// and the pair count equal the launched loop's, without a launch per pair or
+// a host synchronisation per batch.
+constexpr int kBottomCta = 1024;
+
+__device__ __forceinline__ unsigned long long cta_max(unsigned long long v,
+                                                      unsigned long long* red) {
+  v = warp_max_u64(v);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) red[wid] = v;
+  __syncthreads();
+  if (wid == 0) {
+    v = lane < (int)(blockDim.x >> 5) ? red[lane] : 0ull;
+    v = warp_max_u64(v);
+    if (lane == 0) red[32] = v;
+  }
+  __syncthreads();
+  const unsigned long long r = red[32];
+  __syncthreads();
+  return r;
+}
+
+// tol = rel_tol * max(max|f|, 1e-300) / 6 of a level in shared memory (NaN
+// in f makes it NaN, as numpy's max does).
+__device__ double cta_level_tol(const double* f, long n, double rel_tol,
+                                unsigned long long* red) {
+  unsigned long long fk = 0;
+  bool nan = false;
+  for (long t = threadIdx.x; t < n; t += blockDim.x) {
+    const unsigned long long x =
+        static_cast<unsigned long long>(__double_as_longlong(f[t])) & 0x7fffffffffffffffULL;
+    if (x > 0x7ff0000000000000ULL) nan = true;
+    else if (x > fk) fk = x;
+  }
+  nan = __syncthreads_or(nan);
+  fk = cta_max(fk, red);
+  double scale = nan ? __longlong_as_double(0x7ff8000000000000LL) : bits_to_double(fk);
+  scale = (1e-300 > scale) ? 1e-300 : scale;  // max(|f|.max(), 1e-300)
+  return __ddiv_rn(__dmul_rn(rel_tol, scale), 6.0);
+}
+
+// One colour of _sweep_rhs over a level in shared memory; returns the
+// largest |update| key (all threads).
+__device__ unsigned long long cta_sweep(double* e, const uint8_t* fx, const double* f,
+                                        long nx, long ny, long nz, double omega, int colour,
+                                        unsigned long long* red) {
+  const long half = nz / 2 + 1;  // slots of one colour in a row
+  unsigned long long mb = 0;
+  for (long t = threadIdx.x; t < nx * ny * half; t += blockDim.x) {
+    const long ij = t / half, kk = t - ij * half;
+    const long i = ij / ny, j = ij - i * ny;
+    const long k = 2 * kk + ((i + j + colour) & 1);
+    if (k >= nz) continue;
+    const long p = (i * ny + j) * nz + k;
+    if (fx[p]) continue;
+    const Nb nb = neighbours(i, j, k, nx, ny, nz);
+    double v[6];
+    load6(e, nb, v);
+    const double old = e[p];
+    const double nv = div6(__dsub_rn(sum6(v), f[p]));
+    const double nw = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(nv, old)));
+    const unsigned long long x = absbits(__dsub_rn(nw, old));
+    if (x > mb) mb = x;
+    e[p] = nw;
+  }
+  __syncthreads();
+  return cta_max(mb, red);
+}
+
+// The bottom: e = 0; SOR pairs at omega until the larger of a pair's two
+// max |update| is below 0.02 * tol, at most max_pairs pairs.
+__device__ void cta_bottom(double* e, const uint8_t* fx, const double* f, long nx, long ny,
+                           long nz, double rel_tol, double omega, long max_pairs,
+                           unsigned long long* red) {
+  const long n = nx * ny * nz;
+  for (long t = threadIdx.x; t < n; t += blockDim.x) e[t] = 0.0;
+  const double tol = __dmul_rn(0.02, cta_level_tol(f, n, rel_tol, red));
+  for (long pr = 0; pr < max_pairs; pr++) {
+    const unsigned long long k0 = cta_sweep(e, fx, f, nx, ny, nz, omega, 0, red);
+    const unsigned long long k1 = cta_sweep(e, fx, f, nx, ny, nz, omega, 1, red);
+    if (bits_to_double(k0 > k1 ? k0 : k1) < tol) break;
+  }
+}
+
+__global__ void __launch_bounds__(kBottomCta)
+k_bottom_err(double* __restrict__ e_out, const uint8_t* __restrict__ fixed_g,
+             const double* __restrict__ f_g, long nx, long ny, long nz, double rel_tol,
+             double omega, long max_pairs) {
+  extern __shared__ double sm[];
+  __shared__ unsigned long long red[33];
+  const long n = nx * ny * nz;
+  double* e = sm;
+  double* f = sm + n;
+  uint8_t* fx = reinterpret_cast<uint8_t*>(sm + 2 * n);
+  for (long t = threadIdx.x; t < n; t += blockDim.x) {
+    f[t] = f_g[t];
+    fx[t] = fixed_g[t];
+  }
+  __syncthreads();
+  cta_bottom(e, fx, f, nx, ny, nz, rel_tol, omega, max_pairs, red);
+  __syncthreads();
+  for (long t = threadIdx.x; t < n; t += blockDim.x) e_out[t] = e[t];
+}
+
+// multigrid3d._residual_rhs (multigrid3d.py:394-417).
+__global__ void __launch_bounds__(kThreads)
+k_residual_rhs(const double* __restrict__ e, const uint8_t* __restrict__ fixed,
+               const double* __restrict__ f, FlatGeom g,
+               double* __restrict__ out) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= g.total) return;
+  const uint32_t ij = fdiv(t, g.div_nz);
+  const uint32_t k = t - ij * g.div_nz.d;
+  const uint32_t i = fdiv(ij, g.div_ny);
+  const uint32_t j = ij - i * g.div_ny.d;
+  double r = 0.0;
+  if (!fixed[t]) {
+    const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
+    double v[6];
+    load6(e, n, v);
+    r = __dsub_rn(__dsub_rn(sum6(v), __dmul_rn(6.0, e[t])), f[t]);
+  }
+  out[t] = r;
+}
+
+__global__ void __launch_bounds__(kThreads)
+k_restrict(const double* __restrict__ fine, long nx, long ny, long nz,
+           double* __restrict__ out, FlatGeom c, int neg4) {
+  const uint32_t t = blockIdx.x * kThreads + threadIdx.x;
+  if (t >= c.total) return;
+  const uint32_t ij = fdiv(t, c.div_nz);
+  const long kc = t - ij * c.div_nz.d;
+  const long ic = fdiv(ij, c.div_ny);
+  const long jc = ij - ic * c.div_ny.d;
+  out[t] = restrict_node(fine, nx, ny, nz, ic, jc, kc, neg4);
 }
 
 // multigrid3d._prolong_add_njit (multigrid3d.py:458-499).
