@@ -47,6 +47,9 @@ const char *ig_last_error(void);
 int ig_abi_version(void);
 /* Number of visible CUDA devices (0 without a GPU; never fails). */
 int ig_device_count(void);
+/* Free bytes of the calling thread's current device (0 without a GPU; no
+ * reference counterpart: sizes concurrent basis solves). */
+long long ig_device_free_bytes(void);
 
 /* ---- cooperative stop (multigrid3d.py:42, 61-79) ----------------------
  * Replaces the threading.Event _STOP: request_stop() / clear_stop() set and

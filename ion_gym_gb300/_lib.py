@@ -81,6 +81,7 @@ SIGNATURES = {
     "ig_shape_xsection": (_i, [_i, _p, _i, _p, _i, _p, _l, _p, _l, _p]),
     "ig_shapes_label": (_i, [_p, _i, _p, _ll, _p, _ll, _p, _i, _l, _l, _l, _p,
                              _p, _p, _p]),
+    "ig_device_free_bytes": (_ll, []),
     "ig_unit_bases_dev": (_i, [_p, _ll, _d, _p, _p]),
     "ig_superpose_dev": (_i, [_p, _i, _i, _p, _p, _ll, _p, _ll, _p]),
     "ig_field_aware_dev": (_i, [_p, _i, _ll, _i, _p, _l, _l, _l, _d, _i, _p,

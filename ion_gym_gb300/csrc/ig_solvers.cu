@@ -995,3 +995,17 @@ int ig_err_sweep_dev(double* e, const uint8_t* fixed, const float* theta,
 }
 
 }  // extern "C"
+
+extern "C" long long ig_device_free_bytes(void) {
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+    cudaGetLastError();
+    return 0;
+  }
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return (long long)free_b;
+}

@@ -12,6 +12,7 @@ float64 bits.  The stop flag is shared with the library, which polls it where
 the reference polls _STOP: twice per V-cycle and between bases.
 """
 import threading
+import os
 import time
 
 import numpy as np
@@ -250,6 +251,26 @@ def _record_solve(n_nodes, seconds):
     record_solve("mg", n_nodes, basis_s=seconds)
 
 
+# Bases solved at once by solve_bases_mg: each runs on its own host thread
+# and CUDA stream, so the latency-bound coarse levels of one basis overlap
+# the others' work.  Independent problems: every basis keeps its bits.
+BASIS_CONCURRENCY = int(os.environ.get("IG_BASIS_CONCURRENCY", "4"))
+
+
+def _basis_workers(n_bases, n_nodes):
+    """Concurrent basis solves that fit in free device memory (about 32
+    bytes per node each: the potential, its mask and value staging, and the
+    V-cycle's error levels)."""
+    w = max(1, min(BASIS_CONCURRENCY, n_bases))
+    try:
+        free = _lib.lib().ig_device_free_bytes()
+    except Exception:
+        free = 0
+    if free > 0:
+        w = max(1, min(w, int(free * 0.8) // max(32 * n_nodes, 1)))
+    return w
+
+
 def solve_bases_mg(masks, scene=None, mirror=(False, False, False),
                    v_basis=1e4, tol=1e-6, verbose=False,
                    stencil="ghost_linear", theta=None, only=None):
@@ -257,7 +278,10 @@ def solve_bases_mg(masks, scene=None, mirror=(False, False, False),
     index order, the V-cycle on the metal union with that electrode at
     v_basis and the rest at 0.  Raises SolveInterrupted between bases after
     request_stop(), and refuses to return a basis whose delta is not below
-    tol."""
+    tol.  Up to BASIS_CONCURRENCY bases run at once (each on its own
+    stream); progress lines, refusals and the returned dict follow the
+    electrode order exactly as a one-at-a-time loop gives them."""
+    from concurrent.futures import ThreadPoolExecutor
     metal = _union(masks)
     th = theta
     if th is None and scene is not None:
@@ -269,43 +293,66 @@ def solve_bases_mg(masks, scene=None, mirror=(False, False, False),
     mu = as_mask(metal)
     items = sorted(masks.items())
     n = len(items)
+    todo = [(j, i, m) for j, (i, m) in enumerate(items, start=1)
+            if only is None or i in only]
     out = {}
     L = _lib.lib()
-    try:
-        for j, (i, m) in enumerate(items, start=1):
-            if only is not None and i not in only:
-                continue
+
+    def one(i, m):
+        t0 = time.time()
+        phi = np.empty(shape)
+        sw = _lib.ctypes.c_long(0)
+        d = _lib.ctypes.c_double(0.0)
+        cyc = _lib.ctypes.c_int(0)
+        prev = _lib.ctypes.c_double(0.0)
+        st = L.ig_solve_basis_vmg(
+            ptr(mu), ptr(as_mask(m)), float(v_basis), ptr(th), *shape,
+            float(tol), 60, 3, 3, code, float(bom), ptr(phi),
+            _lib.ctypes.byref(sw), _lib.ctypes.byref(d),
+            _lib.ctypes.byref(cyc), _lib.ctypes.byref(prev))
+        return st, phi, sw.value, d.value, cyc.value, prev.value, time.time() - t0
+
+    workers = _basis_workers(len(todo), metal.size)
+    pool = ThreadPoolExecutor(max_workers=workers)
+    futs = {}
+    nxt = 0
+
+    def fill(upto):
+        nonlocal nxt
+        while nxt < len(todo) and nxt < upto:
             if _STOP.is_set():
-                raise SolveInterrupted(
-                    f"stopped after {j - 1} of {n} electrodes")
-            t0 = time.time()
+                return
+            _, i, m = todo[nxt]
+            futs[nxt] = pool.submit(one, i, m)
+            nxt += 1
+
+    try:
+        fill(workers)
+        for q, (j, i, m) in enumerate(todo):
+            if q not in futs:
+                raise SolveInterrupted(f"stopped after {j - 1} of {n} electrodes")
             print(f"  [{time.strftime('%H:%M:%S')}] solving electrode {j} of "
                   f"{n} (basis {i}) ...", flush=True)
-            phi = np.empty(shape)
-            sw = _lib.ctypes.c_long(0)
-            d = _lib.ctypes.c_double(0.0)
-            cyc = _lib.ctypes.c_int(0)
-            prev = _lib.ctypes.c_double(0.0)
-            st = L.ig_solve_basis_vmg(
-                ptr(mu), ptr(as_mask(m)), float(v_basis), ptr(th), *shape,
-                float(tol), 60, 3, 3, code, float(bom), ptr(phi),
-                _lib.ctypes.byref(sw), _lib.ctypes.byref(d),
-                _lib.ctypes.byref(cyc), _lib.ctypes.byref(prev))
+            st, phi, swv, dv, cycv, prevv, secs = futs.pop(q).result()
             _lib.check(st, "solve_bases_mg")
-            phi, swv, dv = _vmg_outcome(st, shape, tol, 60, sw.value,
-                                        d.value, cyc.value, prev.value, phi,
-                                        False)
+            phi, swv, dv = _vmg_outcome(st, shape, tol, 60, swv, dv, cycv, prevv,
+                                        phi, False)
             print(f"  electrode {j} of {n}: {swv} sweeps, delta {dv:.2e} V "
-                  f"({time.time() - t0:.0f}s)", flush=True)
+                  f"({secs:.0f}s)", flush=True)
             if dv >= tol and not np.isnan(dv):
                 raise SolveNotConverged(
                     f"basis {i}: delta {dv:.3e} V >= tol {tol:.1e} came back "
                     f"without a refusal; refusing to cache it.")
             out[i] = phi
-            _record_solve(metal.size, time.time() - t0)
+            _record_solve(metal.size, secs)
+            fill(q + 1 + workers)
     except KeyboardInterrupt:
         raise SolveInterrupted(f"interrupted during electrode solve "
                                f"(completed {len(out)} of {n})")
+    finally:
+        for f in futs.values():
+            f.cancel()
+        pool.shutdown(wait=True)
     return out
 
 
