@@ -488,12 +488,15 @@ def run_uneven(a):
         with MixedSession(fixed, 1) as s:
             return s.solve_values(val, 1e-9)
 
-    workers = 8
+    # largest geometries first (longest-processing-time order), so the
+    # small ones fill the device while the last large ones finish
+    order = sorted(range(len(decks)), key=lambda q: -int(sides[q]) ** 3)
+    workers = a.workers if a.workers > 4 else 12
     with cf.ThreadPoolExecutor(workers) as ex:
         list(ex.map(solve, decks[:workers]))              # warm-up
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        list(ex.map(solve, decks))
+        list(ex.map(solve, [decks[q] for q in order]))
         el = time.perf_counter() - t0
     nodes = sum(int(s) ** 3 for s in sides)
     print(json.dumps({
@@ -504,7 +507,8 @@ def run_uneven(a):
         "data": "synthetic (64 seeded random decks)",
         "config": {"workload": "uneven_batch_64_mixed", "sides":
                    [int(s) for s in sides], "nodes": nodes,
-                   "accuracy_of_span": 1e-9, "concurrent_sessions": workers}}),
+                   "accuracy_of_span": 1e-9, "concurrent_sessions": workers,
+                   "order": "largest grid first"}}),
         flush=True)
 
 

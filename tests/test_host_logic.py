@@ -151,3 +151,59 @@ def test_no_gpu_means_a_loud_error():
     f[0] = True
     with pytest.raises(RuntimeError, match="no CUDA device"):
         S.solve3d(f, np.where(f, 1.0, 0.0))
+
+
+def test_concurrent_basis_door_keeps_the_serial_order(monkeypatch, capsys):
+    """The basis door runs bases on several threads; with a fake library
+    whose solves finish out of order, the progress lines, the returned dict
+    and the first refusal (in electrode order) are those of a serial loop."""
+    import ctypes
+    import random
+    import time as _t
+    from ion_gym_gb300 import _lib
+    from ion_gym_gb300.physics import multigrid3d as M
+
+    shape = (5, 6, 7)
+    masks = {k: np.zeros(shape, bool) for k in (1, 2, 3, 4, 5)}
+    for k, m in masks.items():
+        m[k - 1, 0, 0] = True
+    rnd = random.Random(3)
+    bad = {4}
+
+    class FakeLib:
+        def ig_solve_basis_vmg(self, mu, mk, v, th, nx, ny, nz, tol, mc, n1, n2,
+                               code, bom, phi_p, sw, d, cyc, prev):
+            m = np.ctypeslib.as_array(ctypes.cast(mk, ctypes.POINTER(ctypes.c_uint8)),
+                                      shape=(nx * ny * nz,))
+            k = int(np.argmax(m) // (ny * nz)) + 1
+            _t.sleep(rnd.random() * 0.05)
+            vals = np.full(nx * ny * nz, float(k))
+            ctypes.memmove(phi_p, vals.ctypes.data, vals.nbytes)
+            sw._obj.value = 10 * k
+            d._obj.value = (2 * tol) if k in bad else tol / 2
+            cyc._obj.value = 3
+            prev._obj.value = 0.0
+            return _lib.IG_OK
+
+        def ig_device_free_bytes(self):
+            return 1 << 34
+
+        def ig_clear_stop(self):
+            pass
+
+        def ig_request_stop(self):
+            pass
+
+    M.clear_stop()
+    monkeypatch.setattr(_lib, "lib", lambda: FakeLib())
+    monkeypatch.setattr(M, "BASIS_CONCURRENCY", 3)
+    with pytest.raises(M.SolveNotConverged, match="basis 4"):
+        M.solve_bases_mg(masks, tol=1e-3)
+    lines = [ln for ln in capsys.readouterr().out.splitlines() if "electrode" in ln]
+    assert [ln.split("electrode ")[1].split(" ")[0] for ln in lines] == \
+        ["1", "1", "2", "2", "3", "3", "4", "4"]
+    bad.clear()
+    out = M.solve_bases_mg(masks, tol=1e-3, only={2, 3, 5})
+    assert list(out) == [2, 3, 5]
+    for k, phi in out.items():
+        assert phi.shape == shape and np.all(phi == k)
