@@ -287,6 +287,10 @@ def run_ours(a):
             for _ in range(a.steps):
                 phi_m = sess.solve_values(val, accuracy=1e-9)
             el_m = time.perf_counter() - tm
+            import ctypes as _ct
+            gms, gby = _ct.c_double(0), _ct.c_double(0)
+            L.ig_mixed_time_gs(sess._h, 1, 20, _ct.byref(gms), _ct.byref(gby))
+            gs_gbs = gby.value / (gms.value * 1e-3) / 1e9
             line["mixed"] = {
                 "value": a.steps / el_m, "unit": "solves/s",
                 "path": "MixedSession.solve_values, host buffers in and out",
@@ -294,7 +298,12 @@ def run_ours(a):
                 "refinement_steps": sess.last_steps,
                 "over_fp64_e2e": (a.steps / el_m) / (a.steps / el_e2e),
                 "max_abs_diff_vs_fp64_cascadic_of_span":
-                    float(np.abs(phi_m[0] - phi64).max()) / 2.0}
+                    float(np.abs(phi_m[0] - phi64).max()) / 2.0,
+                "roofline": {"bound": "hbm", "kernel": "k_gs4 (FP32 split "
+                             "red-black Gauss-Seidel, 13 B per updated node)",
+                             "achieved": gs_gbs, "peak": peak, "unit": "GB/s",
+                             "frac": gs_gbs / peak if peak else None,
+                             "avg_launch_us": 1e3 * gms.value}}
     if rank == 0 and ws == 1 and not a.no_cpu:
         g, pairs, secs, thr = cpu_sample(fixed, seconds=a.cpu_seconds)
         line["cpu_baseline"] = {
