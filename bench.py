@@ -107,10 +107,8 @@ class Clocks:
 
 
 def dist():
-    ws = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return ws, rank, local
+    from ion_gym_gb300 import replicas
+    return replicas.world()
 
 
 def cpu_sample(fixed, seconds=15.0, max_pairs=400):
@@ -158,11 +156,10 @@ def load_profile_traffic():
 
 def run_ours(a):
     import torch
+    from ion_gym_gb300 import replicas
     ws, rank, local = dist()
     torch.cuda.set_device(local)
-    if ws > 1:
-        import torch.distributed as tdist
-        tdist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    replicas.init("nccl", torch.device("cuda", local))
     from ion_gym_gb300 import build as B, _lib
     if not os.path.exists(B.LIB):
         B.build()
@@ -187,9 +184,7 @@ def run_ours(a):
                                           9, CHECK_EVERY, out=phi_h)
 
     def barrier():
-        if ws > 1:
-            import torch.distributed as tdist
-            tdist.barrier()
+        replicas.barrier()
         torch.cuda.synchronize()
 
     info = None
@@ -215,23 +210,14 @@ def run_ours(a):
     nl = ctypes.c_long(0)
     nodes = ctypes.c_long(0)
     L.ig_prof_read(ctypes.byref(ms), ctypes.byref(nl), ctypes.byref(nodes))
-    if ws > 1:
-        import torch.distributed as tdist
-        t = torch.tensor([el], device="cuda", dtype=torch.float64)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        el = float(t.item())
+    el = replicas.max_over_ranks(el, "cuda")
     # e2e: public API on pinned host buffers, copies inside the timed region
     barrier()
     t1 = time.perf_counter()
     for _ in range(a.steps):
         solve_host()
     barrier()
-    el_e2e = time.perf_counter() - t1
-    if ws > 1:
-        import torch.distributed as tdist
-        t = torch.tensor([el_e2e], device="cuda", dtype=torch.float64)
-        tdist.all_reduce(t, op=tdist.ReduceOp.MAX)
-        el_e2e = float(t.item())
+    el_e2e = replicas.max_over_ranks(time.perf_counter() - t1, "cuda")
 
     _, fine_pairs, relres, total_pairs = info
     lups = nodes.value / a.steps                      # LUPs per solve
