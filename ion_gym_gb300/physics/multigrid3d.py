@@ -254,7 +254,7 @@ def _record_solve(n_nodes, seconds):
 # Bases solved at once by solve_bases_mg: each runs on its own host thread
 # and CUDA stream, so the latency-bound coarse levels of one basis overlap
 # the others' work.  Independent problems: every basis keeps its bits.
-BASIS_CONCURRENCY = int(os.environ.get("IG_BASIS_CONCURRENCY", "4"))
+BASIS_CONCURRENCY = int(os.environ.get("IG_BASIS_CONCURRENCY", "8"))
 
 
 def _basis_workers(n_bases, n_nodes):
