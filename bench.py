@@ -139,10 +139,10 @@ def lups_per_solve(level_pairs):
     return sum(int(np.prod(s)) * p for s, p in zip(shapes, level_pairs))
 
 
-def load_profile_traffic():
+def load_profile_traffic(name="sweep_f64_quad257.md"):
     """dram bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/), or None."""
-    p = os.path.join(ROOT, "profiles", "sweep_f64_quad257.md")
+    summary (profiles/<name>: its `dram_bytes_per_launch:` line), or None."""
+    p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
@@ -441,7 +441,7 @@ def run_rings(a):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s",
                      "frac": achieved / peak if peak else None,
-                     "traffic": None,
+                     "traffic": load_profile_traffic("k_gs4_ring_stack.md"),
                      "kernel": "k_gs (FP32 red-black split Gauss-Seidel)",
                      "avg_launch_us": 1e3 * ms.value},
         "clocks": ck,
@@ -697,7 +697,9 @@ def run_compose(a):
                         "GB/s": (fld_b - n) / (times["plain"] * 1e-3) / 1e9}},
         "roofline": {"bound": "hbm", "achieved": dom[1], "peak": peak,
                      "unit": "GB/s", "frac": dom[1] / peak if peak else None,
-                     "traffic": None, "kernel": dom[0],
+                     "traffic": load_profile_traffic("field_compose_ring_stack.md")
+                     if dom[0].startswith("k_field32") else None,
+                     "kernel": dom[0],
                      "avg_launch_us": 1e3 * dom[3] / a.steps},
         "clocks": ck,
     }
