@@ -173,7 +173,7 @@ __device__ __forceinline__ void load6(const double* __restrict__ a, const Nb& n,
 }
 
 // solver3d._sweep (solver3d.py:131-198).
-template <int KIND, bool CTL>
+template <int KIND, bool CTL, bool DELTA = true>
 __global__ void __launch_bounds__(kThreads)
 k_sweep(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
         const float* __restrict__ th, SweepGeom g, double omega, int colour,
@@ -206,12 +206,14 @@ k_sweep(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
           q = __ddiv_rn(num, den);
         }
         const double nw = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(q, old)));
-        mb = absbits(__dsub_rn(nw, old));
+        if (DELTA) mb = absbits(__dsub_rn(nw, old));
         phi[p] = nw;
       }
     }
   }
-  block_max_to(mb, dslot);
+  // without a slot (DELTA false) nobody reads the max |update|: skip the
+  // subtraction and the block reduction
+  if (DELTA) block_max_to(mb, dslot);
 }
 
 // multigrid3d._residual (multigrid3d.py:305-354): num - den*phi, 0 at fixed.
@@ -713,8 +715,10 @@ void launch_sweep(cudaStream_t s, double* phi, const uint8_t* fixed,
 #define IG_SWEEP(K)                                                              \
   if (ctl) k_sweep<K, true><<<nb, kThreads, 0, s>>>(phi, fixed, th, g, omega,    \
                                                     colour, dslot, ctl, lp);     \
-  else k_sweep<K, false><<<nb, kThreads, 0, s>>>(phi, fixed, th, g, omega,       \
-                                                 colour, dslot, ctl, lp);
+  else if (dslot) k_sweep<K, false><<<nb, kThreads, 0, s>>>(phi, fixed, th, g,   \
+                                                 omega, colour, dslot, ctl, lp); \
+  else k_sweep<K, false, false><<<nb, kThreads, 0, s>>>(phi, fixed, th, g,       \
+                                                 omega, colour, dslot, ctl, lp);
   if (kind == kPlain) { IG_SWEEP(kPlain) }
   else if (kind == kThetaGhost) { IG_SWEEP(kThetaGhost) }
   else { IG_SWEEP(kThetaSW) }

@@ -425,13 +425,12 @@ VmgOut vmg_loop(ThreadCtx& c, FineGrid& g, VCycle& v, double tol,
   long sweeps = 0;
   double prev = std::numeric_limits<double>::infinity();
   double cycle_d = std::numeric_limits<double>::infinity();
-  unsigned long long* sl = v.slots.p;
   for (int cyc = 0; cyc < max_cycles; cyc++) {
     if (g_stop.load()) return {IG_INTERRUPTED, sweeps, prev, cyc, prev};
     CK(cudaMemcpyAsync(phi_c0.p, g.phi.p, n * 8, cudaMemcpyDeviceToDevice, c.s));
     for (int q = 0; q < v.nu1; q++) {
-      launch_sweep(c.s, g.phi.p, g.fixed.p, g.thp(), kind, g.d, 1.0, 0, sl, nullptr, 0);
-      launch_sweep(c.s, g.phi.p, g.fixed.p, g.thp(), kind, g.d, 1.0, 1, sl, nullptr, 0);
+      launch_sweep(c.s, g.phi.p, g.fixed.p, g.thp(), kind, g.d, 1.0, 0, nullptr, nullptr, 0);
+      launch_sweep(c.s, g.phi.p, g.fixed.p, g.thp(), kind, g.d, 1.0, 1, nullptr, nullptr, 0);
       sweeps++;
     }
     CK(cudaGetLastError());
@@ -445,8 +444,8 @@ VmgOut vmg_loop(ThreadCtx& c, FineGrid& g, VCycle& v, double tol,
     solve_err(c, v, 0);
     launch_prolong_add(c.s, e0.e.p, e0.d, g.phi.p, g.fixed.p, g.d);
     for (int q = 0; q < v.nu2; q++) {
-      launch_sweep(c.s, g.phi.p, g.fixed.p, g.thp(), kind, g.d, 1.0, 0, sl, nullptr, 0);
-      launch_sweep(c.s, g.phi.p, g.fixed.p, g.thp(), kind, g.d, 1.0, 1, sl, nullptr, 0);
+      launch_sweep(c.s, g.phi.p, g.fixed.p, g.thp(), kind, g.d, 1.0, 0, nullptr, nullptr, 0);
+      launch_sweep(c.s, g.phi.p, g.fixed.p, g.thp(), kind, g.d, 1.0, 1, nullptr, nullptr, 0);
       sweeps++;
     }
     for (int a : sym) launch_sym_project(c.s, g.phi.p, g.d, a);
@@ -787,8 +786,8 @@ int ig_cascadic_relres(const uint8_t* fixed, const double* val, long nx,
         const int chunk = (int)std::min<long>(check_every, max_sweeps - pairs);
         if (prof) CK(cudaEventRecord(c.ev0, c.s));
         for (int q = 0; q < chunk; q++) {
-          launch_sweep(c.s, nxt.p, M.fixed.p, nullptr, kPlain, M.d, om, 0, red.p, nullptr, 0);
-          launch_sweep(c.s, nxt.p, M.fixed.p, nullptr, kPlain, M.d, om, 1, red.p, nullptr, 0);
+          launch_sweep(c.s, nxt.p, M.fixed.p, nullptr, kPlain, M.d, om, 0, nullptr, nullptr, 0);
+          launch_sweep(c.s, nxt.p, M.fixed.p, nullptr, kPlain, M.d, om, 1, nullptr, nullptr, 0);
         }
         CK(cudaGetLastError());
         if (prof) {
