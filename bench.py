@@ -413,7 +413,9 @@ def run_rings(a):
     el_e2e = time.perf_counter() - t1
     # the FP64 drop-in on the same bases
     tf = time.perf_counter()
-    fp = MG.solve_bases_mg(masks, v_basis=V, tol=ACC * V, only=set(rings))
+    import contextlib
+    with contextlib.redirect_stdout(sys.stderr):    # the door's progress lines
+        fp = MG.solve_bases_mg(masks, v_basis=V, tol=ACC * V, only=set(rings))
     el_fp = time.perf_counter() - tf
     err = max(float(np.abs(phi[b] - fp[i]).max()) / V
               for b, i in enumerate(rings))

@@ -62,8 +62,10 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
   return v;
 }
 
-// Block-wide max of a 64-bit key, then one atomicMax into *dst.
-// Every thread of the block must call it.
+// Block-wide max of a 64-bit key, then one atomicMax into *dst -- only when
+// it beats the value already there, so the tens of thousands of blocks of a
+// launch do not all queue atomics on one address.  Every thread of the
+// block must call it.
 __device__ __forceinline__ void block_max_to(unsigned long long v,
                                              unsigned long long* dst) {
   __shared__ unsigned long long red[32];
@@ -75,7 +77,8 @@ __device__ __forceinline__ void block_max_to(unsigned long long v,
     const int nw = (blockDim.x + 31) >> 5;
     v = lane < nw ? red[lane] : 0ULL;
     v = warp_max_u64(v);
-    if (lane == 0 && v) atomicMax(dst, v);
+    if (lane == 0 && v && v > *reinterpret_cast<volatile unsigned long long*>(dst))
+      atomicMax(dst, v);
   }
 }
 
