@@ -53,13 +53,14 @@ __device__ __forceinline__ unsigned long long absbits(double d) {
   return b > 0x7ff0000000000000ULL ? 0ULL : b;
 }
 
+// Warp max of a 64-bit key with two 32-bit warp reductions (REDUX): the
+// largest high word, then the largest low word among the lanes holding it.
+// Every lane of the warp must call it.
 __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
-    v = w > v ? w : v;
-  }
-  return v;
+  const unsigned hi = __reduce_max_sync(0xffffffffu, (unsigned)(v >> 32));
+  const unsigned lo =
+      __reduce_max_sync(0xffffffffu, (unsigned)(v >> 32) == hi ? (unsigned)v : 0u);
+  return ((unsigned long long)hi << 32) | lo;
 }
 
 // Block-wide max of a 64-bit key, then one atomicMax into *dst -- only when
