@@ -266,12 +266,14 @@ def run_ours(a):
         # buffers in and out like e2e, against the FP64 cascadic result
         from ion_gym_gb300.physics.mixed import MixedSession
         phi64 = phi_h.numpy().copy()
+        val_p = val_h.numpy()                        # pinned, as for e2e
+        out_p = torch.empty(val.shape, dtype=torch.float64).pin_memory().numpy()
         with MixedSession(fixed, 1) as sess:
-            sess.solve_values(val, accuracy=1e-9)
+            sess.solve_values(val_p, accuracy=1e-9, out=out_p, span=2.0)
             torch.cuda.synchronize()
             tm = time.perf_counter()
             for _ in range(a.steps):
-                phi_m = sess.solve_values(val, accuracy=1e-9)
+                phi_m = sess.solve_values(val_p, accuracy=1e-9, out=out_p, span=2.0)
             el_m = time.perf_counter() - tm
             import ctypes as _ct
             gms, gby = _ct.c_double(0), _ct.c_double(0)
@@ -279,7 +281,7 @@ def run_ours(a):
             gs_gbs = gby.value / (gms.value * 1e-3) / 1e9
             line["mixed"] = {
                 "value": a.steps / el_m, "unit": "solves/s",
-                "path": "MixedSession.solve_values, host buffers in and out",
+                "path": "MixedSession.solve_values, pinned host buffers in and out",
                 "accuracy_of_span": 1e-9,
                 "refinement_steps": sess.last_steps,
                 "over_fp64_e2e": (a.steps / el_m) / (a.steps / el_e2e),
@@ -369,7 +371,7 @@ def run_rings(a):
     import torch
     from ion_gym_gb300 import _lib
     from ion_gym_gb300.workloads import ring_stack
-    from ion_gym_gb300.physics.mixed import MixedSession, solve_bases_mixed
+    from ion_gym_gb300.physics.mixed import MixedSession
     from ion_gym_gb300.physics import multigrid3d as MG
     torch.cuda.set_device(0)
     L = _lib.lib()
@@ -406,10 +408,15 @@ def run_rings(a):
     L.ig_mixed_time_gs(sess._h, len(rings), 20, ctypes.byref(ms),
                        ctypes.byref(by))
     achieved = by.value / (ms.value * 1e-3) / 1e9
-    # e2e through the public API (host masks in, host bases out)
+    # e2e through the public API: the session's solve from pinned host masks
+    # to pinned host potentials (upload and download inside the timed region)
+    masks_h = torch.empty(stack.shape, dtype=torch.uint8).pin_memory().numpy()
+    masks_h[...] = np.stack([masks[i] for i in rings]).view(np.uint8)
+    out_h = torch.empty(out.shape, dtype=torch.float64).pin_memory().numpy()
+    sess.solve_bases(masks_h, V, ACC, out=out_h)
     t1 = time.perf_counter()
     for _ in range(a.steps):
-        solve_bases_mixed(masks, V, ACC, only=set(rings))
+        sess.solve_bases(masks_h, V, ACC, out=out_h)
     el_e2e = time.perf_counter() - t1
     # the FP64 drop-in on the same bases
     tf = time.perf_counter()
@@ -437,7 +444,7 @@ def run_rings(a):
         "mixed_over_fp64": (len(rings) * a.steps / el) / (len(rings) / el_fp),
         "max_abs_diff_vs_fp64_of_span": err,
         "e2e": {"value": len(rings) * a.steps / el_e2e, "unit": "solves/s",
-                "h2d_bytes_per_step": n * (len(masks) + 1),
+                "h2d_bytes_per_step": n * len(rings),
                 "d2h_bytes_per_step": n * 8 * len(rings)},
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,

@@ -70,13 +70,19 @@ class MixedSession:
 
     def solve_bases(self, masks, v_basis=1e4, accuracy=1e-9, max_steps=40,
                     out=None):
-        """masks: sequence of (nx,ny,nz) bool, or a CUDA uint8 tensor
-        (B, nx, ny, nz) already on the device -> potentials (B, nx, ny, nz)
-        float64: a numpy array, or `out` (a CUDA float64 tensor) when
-        given."""
+        """masks: a sequence of (nx,ny,nz) bool arrays, a (B, nx, ny, nz)
+        uint8 / bool numpy array (used in place: pinned host memory makes
+        the upload fast), or a CUDA uint8 tensor already on the device ->
+        potentials (B, nx, ny, nz) float64: a new numpy array, or `out` (a
+        C-contiguous float64 numpy array -- pinned for a fast download -- or
+        CUDA tensor) when given."""
         if type(masks).__module__.startswith("torch"):
             B = int(masks.shape[0])
             mptr = ctypes.c_void_p(masks.data_ptr())
+        elif (isinstance(masks, np.ndarray) and masks.ndim == 4
+              and masks.dtype in (np.uint8, np.bool_) and masks.flags.c_contiguous):
+            B = int(masks.shape[0])
+            mptr = ptr(masks)
         else:
             B = len(masks)
             stack = np.empty((B,) + self.shape, np.uint8)
@@ -86,6 +92,13 @@ class MixedSession:
         if out is None:
             phi = np.empty((B,) + self.shape)
             pptr = ptr(phi)
+        elif isinstance(out, np.ndarray):
+            if out.dtype != np.float64 or not out.flags.c_contiguous or \
+                    out.shape != (B,) + self.shape:
+                raise ValueError("solve_bases: out must be a C-contiguous float64 "
+                                 f"array of shape {(B,) + self.shape}")
+            phi = out
+            pptr = ptr(out)
         else:
             phi = out
             pptr = ctypes.c_void_p(out.data_ptr())
@@ -99,18 +112,29 @@ class MixedSession:
         self.last_steps = int(steps.value)
         return phi
 
-    def solve_values(self, vals, accuracy=1e-9, max_steps=40):
+    def solve_values(self, vals, accuracy=1e-9, max_steps=40, out=None,
+                     span=None):
         """vals: (P, nx, ny, nz) Dirichlet values (read at the metal nodes)
-        -> array (P, nx, ny, nz); accuracy is relative to each problem's
-        span of Dirichlet values (at least 1 V)."""
+        -> array (P, nx, ny, nz); accuracy is relative to the span of the
+        Dirichlet values (max - min of vals, at least 1 V; pass `span` when
+        it is known, to skip the host pass over vals).  `out`: a
+        C-contiguous float64 array of that shape to fill (pinned host memory
+        makes the download fast)."""
         vals = np.ascontiguousarray(vals, np.float64)
         if vals.ndim == 3:
             vals = vals[None]
         P = vals.shape[0]
-        phi = np.empty_like(vals)
+        if out is None:
+            phi = np.empty_like(vals)
+        else:
+            if out.dtype != np.float64 or not out.flags.c_contiguous or \
+                    out.size != vals.size:
+                raise ValueError("solve_values: out must be a C-contiguous float64 "
+                                 f"array of {vals.size} values")
+            phi = out.reshape(vals.shape)
         steps = ctypes.c_int(0)
         dmax = np.zeros(P)
-        span = max(float(np.ptp(vals)), 1.0)
+        span = max(float(np.ptp(vals)) if span is None else float(span), 1.0)
         st = _lib.lib().ig_mixed_solve_values(
             self._h, ptr(vals), P, float(accuracy) * span, int(max_steps),
             ptr(phi), ctypes.byref(steps), ptr(dmax))
