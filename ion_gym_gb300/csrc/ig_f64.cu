@@ -5,7 +5,7 @@
 // physics/multigrid3d.py, cited per kernel).  FP64 is the scarce pipe on
 // GB300 (about 1/64 of the FP32 rate), so the kernels spend it only where the
 // reference does: masks, indices, maxima and absolute values run on the
-// integer pipe, and the theta == 1 stencil divides by 6 in two FP64 operations
+// integer pipe, and the theta == 1 stencil divides by 6 on the integer pipe
 // (ig::div6) instead of a full division.
 //
 // Layout: C-order (nx, ny, nz), z contiguous; theta (6, nx, ny, nz) float32.
@@ -205,7 +205,7 @@ k_sweep(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
           theta_num_den<KIND>(v, th, (size_t)g.nx * g.ny * g.nz, p, num, den);
           q = __ddiv_rn(num, den);
         }
-        const double nw = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(q, old)));
+        const double nw = __dadd_rn(old, omega_step(old, q, omega));
         if (DELTA) mb = absbits(__dsub_rn(nw, old));
         phi[p] = nw;
       }
@@ -277,7 +277,7 @@ k_sweep_rhs(double* __restrict__ e, const uint8_t* __restrict__ fixed,
         load6(e, n, v);
         const double old = e[p];
         const double nv = div6(__dsub_rn(sum6(v), f[p]));
-        const double nw = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(nv, old)));
+        const double nw = __dadd_rn(old, omega_step(old, nv, omega));
         mb = absbits(__dsub_rn(nw, old));
         e[p] = nw;
       }
@@ -432,7 +432,7 @@ __device__ unsigned long long cta_sweep(double* e, const uint8_t* fx, const doub
     load6(e, nb, v);
     const double old = e[p];
     const double nv = div6(__dsub_rn(sum6(v), f[p]));
-    const double nw = __dadd_rn(old, __dmul_rn(omega, __dsub_rn(nv, old)));
+    const double nw = __dadd_rn(old, omega_step(old, nv, omega));
     const unsigned long long x = absbits(__dsub_rn(nw, old));
     if (x > mb) mb = x;
     e[p] = nw;

@@ -114,6 +114,8 @@ __device__ __forceinline__ float4 ld4(const float* p) {
 }
 
 // One float4 group (slots m0..m0+3 of colour c, row ij) of the update.
+// FLAT: the grid has a size-1 axis (per-slot neighbour sums).
+template <bool FLAT>
 __device__ __forceinline__ void gs4_at(float* __restrict__ own, const float* __restrict__ oth,
                                        const float* __restrict__ gp,
                                        const uint8_t* __restrict__ mp, const SGeo& G, int c,
@@ -123,26 +125,35 @@ __device__ __forceinline__ void gs4_at(float* __restrict__ own, const float* __r
   const uchar4 mk = *reinterpret_cast<const uchar4*>(mp + base);
   if (mk.x & mk.y & mk.z & mk.w) return;  // all metal or unused slots
   const float4 gg = ld4(gp + base);
-  const int kmax = 2 * (m0 + 3) + p;
   float q[4];
-  const bool fast = G.nx > 1 && G.ny > 1 && G.nz > 1 && m0 >= 1 && kmax <= G.nz - 2;
-  if (fast) {
+  // Grids with no size-1 axis take the float4 path for every group, the z
+  // faces included, so no warp diverges into a per-slot path at the ends of
+  // its rows.
+  if (!FLAT) {
     const float4 xm = ld4(oth + ((uint32_t)lo_i(i, G.nx) * G.ny + j) * G.H + m0);
     const float4 xp = ld4(oth + ((uint32_t)hi_i(i, G.nx) * G.ny + j) * G.H + m0);
     const float4 ym = ld4(oth + ((uint32_t)i * G.ny + lo_i(j, G.ny)) * G.H + m0);
     const float4 yp = ld4(oth + ((uint32_t)i * G.ny + hi_i(j, G.ny)) * G.H + m0);
     const float4 zc = ld4(oth + base);
-    // z neighbours of slot m: slots m-1+p and m+p of the other colour row
+    // z neighbours of slot m (node k = 2m + p): k-1 is slot m-1+p and k+1
+    // slot m+p of the other colour's row.  Node 0 reflects k-1 to k+1
+    // (slot 0); node nz-1 reflects k+1 to k-1.  The slot past the row's end
+    // (p = 1, last group) only feeds unused slots, which are never written.
     float z[5];
     if (p == 0) {
-      z[0] = oth[base - 1]; z[1] = zc.x; z[2] = zc.y; z[3] = zc.z; z[4] = zc.w;
+      z[0] = m0 > 0 ? oth[base - 1] : zc.x;
+      z[1] = zc.x; z[2] = zc.y; z[3] = zc.z; z[4] = zc.w;
     } else {
-      z[0] = zc.x; z[1] = zc.y; z[2] = zc.z; z[3] = zc.w; z[4] = oth[base + 4];
+      z[0] = zc.x; z[1] = zc.y; z[2] = zc.z; z[3] = zc.w;
+      z[4] = m0 + 4 < G.H ? oth[base + 4] : 0.f;
     }
-    q[0] = ((xm.x + xp.x) + (ym.x + yp.x)) + (z[0] + z[1]);
-    q[1] = ((xm.y + xp.y) + (ym.y + yp.y)) + (z[1] + z[2]);
-    q[2] = ((xm.z + xp.z) + (ym.z + yp.z)) + (z[2] + z[3]);
-    q[3] = ((xm.w + xp.w) + (ym.w + yp.w)) + (z[3] + z[4]);
+    const int utop = G.nz - 1 - p - 2 * m0;  // 2u == utop: node nz-1
+    const float4 s4 = make_float4((xm.x + xp.x) + (ym.x + yp.x), (xm.y + xp.y) + (ym.y + yp.y),
+                                  (xm.z + xp.z) + (ym.z + yp.z), (xm.w + xp.w) + (ym.w + yp.w));
+    const float sx[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+    for (int u = 0; u < 4; u++)
+      q[u] = sx[u] + (z[u] + (2 * u == utop ? z[u] : z[u + 1]));
   } else {
 #pragma unroll
     for (int u = 0; u < 4; u++) {
@@ -166,6 +177,7 @@ __device__ __forceinline__ void gs4_at(float* __restrict__ own, const float* __r
   }
 }
 
+template <bool FLAT>
 __device__ __forceinline__ void gs4_group(float* __restrict__ own, const float* __restrict__ oth,
                                           const float* __restrict__ gp,
                                           const uint8_t* __restrict__ mp, const SGeo& G,
@@ -174,7 +186,7 @@ __device__ __forceinline__ void gs4_group(float* __restrict__ own, const float* 
   const int m0 = 4 * (int)(t - ij * G.dH4.d);
   const int i = (int)fdivu(ij, G.dny);
   const int j = (int)(ij - (uint32_t)i * G.dny.d);
-  gs4_at(own, oth, gp, mp, G, c, omega, ij, i, j, m0);
+  gs4_at<FLAT>(own, oth, gp, mp, G, c, omega, ij, i, j, m0);
 }
 
 // Red-black Gauss-Seidel half-sweep of colour c on the split layout.  Each
@@ -185,7 +197,7 @@ __device__ __forceinline__ void gs4_group(float* __restrict__ own, const float* 
 // blockDim apart so every load instruction stays coalesced.  Groups that
 // touch a face in z, or grids with a size-1 axis, take the per-slot path.
 // NG and the block size are chosen per grid by the session's tuner.
-template <int NG>
+template <int NG, bool FLAT>
 __global__ void k_gs4(float* __restrict__ e, const float* __restrict__ g,
                       const uint8_t* __restrict__ mask, SGeo G, int c, float omega,
                       size_t pstride) {
@@ -199,7 +211,7 @@ __global__ void k_gs4(float* __restrict__ e, const float* __restrict__ g,
 #pragma unroll
   for (int u = 0; u < NG; u++) {
     const uint32_t t = t0 + u * blockDim.x;
-    if (t < nq) gs4_group(own, oth, gp, mp, G, c, omega, t);
+    if (t < nq) gs4_group<FLAT>(own, oth, gp, mp, G, c, omega, t);
   }
 }
 
@@ -207,6 +219,7 @@ __global__ void k_gs4(float* __restrict__ e, const float* __restrict__ g,
 // thread (slots m0..m0+7): one index computation and one mask / z-boundary
 // lookup serve eight slots.  A row with an odd number of groups leaves the
 // second group of its last pair idle.
+template <bool FLAT>
 __global__ void k_gs8(float* __restrict__ e, const float* __restrict__ g,
                       const uint8_t* __restrict__ mask, SGeo G, int c, float omega,
                       size_t pstride) {
@@ -223,8 +236,8 @@ __global__ void k_gs8(float* __restrict__ e, const float* __restrict__ g,
   const uint8_t* mp = mask + (size_t)c * G.csz;
   const int i = (int)fdivu(ij, G.dny);
   const int j = (int)(ij - (uint32_t)i * G.dny.d);
-  gs4_at(own, oth, gp, mp, G, c, omega, ij, i, j, 4 * (int)q0);
-  if (q0 + 1 < H4) gs4_at(own, oth, gp, mp, G, c, omega, ij, i, j, 4 * (int)q0 + 4);
+  gs4_at<FLAT>(own, oth, gp, mp, G, c, omega, ij, i, j, 4 * (int)q0);
+  if (q0 + 1 < H4) gs4_at<FLAT>(own, oth, gp, mp, G, c, omega, ij, i, j, 4 * (int)q0 + 4);
 }
 
 // Residual r = g - A e of colour 0 only, in split layout.  After a red-black
@@ -916,23 +929,32 @@ struct Session {
   // One colour half-sweep of level a for nb problems with the tuned shape.
   void launch_gs(MLevel& a, int c, int nb, float omega) {
     const uint32_t nq = a.G.csz / 4;
+    if (a.G.nx == 1 || a.G.ny == 1 || a.G.nz == 1) {
+      k_gs4<1, true><<<dim3(nblk(nq), nb), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega,
+                                                      a.pstride);
+      return;
+    }
     const unsigned per = (unsigned)(gs_cfg.threads * gs_cfg.ng);
     const dim3 grid((nq + per - 1) / per, nb);
     if (gs_cfg.ng == 8) {
       const uint32_t npair = (uint32_t)a.G.nx * a.G.ny * a.G.dH8.d;
       const dim3 g8((npair + gs_cfg.threads - 1) / gs_cfg.threads, nb);
-      k_gs8<<<g8, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega, a.pstride);
+      k_gs8<false><<<g8, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega,
+                                                 a.pstride);
       return;
     }
     switch (gs_cfg.ng) {
       case 4:
-        k_gs4<4><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega, a.pstride);
+        k_gs4<4, false><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega,
+                                                        a.pstride);
         break;
       case 2:
-        k_gs4<2><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega, a.pstride);
+        k_gs4<2, false><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega,
+                                                        a.pstride);
         break;
       default:
-        k_gs4<1><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega, a.pstride);
+        k_gs4<1, false><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega,
+                                                        a.pstride);
         break;
     }
   }

@@ -26,9 +26,10 @@ def _th(c):
 
 
 def test_div6_is_correctly_rounded():
-    """The two-operation division by 6 of the theta-free sweep equals x/6
-    for values across the whole exponent range (the sweep of a grid whose
-    neighbours all hold x computes (6x)/6 through it)."""
+    """The integer-pipe division by 6 of the theta-free sweep equals x/6
+    for values across the whole exponent range, the significands on either
+    side of 1.5 (where the quotient's scaling changes) and the exponents
+    where the hardware division takes over."""
     from ion_gym_gb300.physics import _device as D
     torch = D._torch()
     rng = np.random.default_rng(5)
@@ -39,7 +40,13 @@ def test_div6_is_correctly_rounded():
     x = x[np.isfinite(x) & (np.abs(x) < 1e300)]
     special = np.array([0.0, -0.0, 5e-324, -5e-324, 1e-310, -2.2e-308, 6.0,
                         -6.0, 3.0, 1e-300, 1e300, 0.5, 1.0 / 3.0])
-    x = np.concatenate([special, special, x])
+    mant = np.array([0, 1, 2, (1 << 51) - 1, 1 << 51, (1 << 51) + 1,
+                     (1 << 52) - 2, (1 << 52) - 1], dtype=np.uint64)
+    ex = np.concatenate([np.arange(1, 9), np.arange(1020, 1030),
+                         np.arange(2040, 2047)]).astype(np.uint64)
+    edge = ((ex[:, None] << np.uint64(52)) | mant[None, :]).ravel()
+    edge = np.concatenate([edge, edge | np.uint64(1 << 63)]).view(np.float64)
+    x = np.concatenate([special, special, edge, x])
     # a 1 x 1 x n grid with every node free: the sweep on colour c reads
     # its two z-neighbours; put x/2 on the neighbours so num = 6 * (x/2) *...
     # Instead drive the residual-free identity directly: sweep_rhs with
@@ -56,6 +63,45 @@ def test_div6_is_correctly_rounded():
     want = 0.0 + 1.0 * ((0.0 - fn) / 6.0 - 0.0)
     even = np.arange(n) % 2 == 0  # colour 0 nodes of a 1x1xn grid
     assert np.array_equal(got[even].view(np.uint64), want[even].view(np.uint64))
+
+
+def test_sor_step_is_exact():
+    """The integer-pipe SOR step RN(omega * RN(nv - old)) equals the FP64
+    expression: old and nv in one binade or adjacent ones, far apart,
+    opposite signs, equal, tiny and huge, for several omegas.  A 1 x 1 x n
+    grid: a colour-0 node sees itself on the four flat-axis legs and its two
+    z-neighbours."""
+    from ion_gym_gb300.physics import _device as D
+    torch = D._torch()
+    rng = np.random.default_rng(17)
+    n = 1_200_001
+    mag = 2.0 ** rng.integers(-900, 900, n)
+    e = rng.uniform(0.5, 2.0, n) * mag * rng.choice([-1.0, 1.0], n)
+    mode = rng.integers(0, 6, n)
+    rel = 10.0 ** rng.uniform(-16, 0, n) * rng.choice([-1.0, 1.0], n)
+    target = e * (1 + rel)
+    target = np.where(mode == 1, e, target)                       # nv == old
+    target = np.where(mode == 2, -e * rng.uniform(0.3, 3, n), target)
+    target = np.where(mode == 3, np.nextafter(e, 2 * e), target)  # one ulp
+    target = np.where(mode == 4, e * 2.0 ** rng.integers(-3, 4, n), target)
+    k = np.arange(n)
+    zm = e[np.where(k > 0, k - 1, 1)]
+    zp = e[np.where(k < n - 1, k + 1, n - 2)]
+    s6 = ((((e + e) + e) + e) + zm) + zp
+    with np.errstate(over="ignore", invalid="ignore"):
+        f = s6 - 6.0 * target
+    f = np.where(np.isfinite(f), f, 0.0)
+    fixed = torch.zeros((1, 1, n), dtype=torch.uint8, device="cuda")
+    even = k % 2 == 0
+    for omega in (1.0, 1.85, 1.2345678901234567, 0.7):
+        et = torch.from_numpy(e.reshape(1, 1, n).copy()).to("cuda")
+        ft = torch.from_numpy(f.reshape(1, 1, n)).to("cuda")
+        D.sweep_rhs(et, fixed, ft, omega, 0)
+        got = et.cpu().numpy().ravel()
+        with np.errstate(over="ignore", invalid="ignore"):
+            want = e + omega * ((s6 - f) / 6.0 - e)
+        assert np.array_equal(got[even].view(np.uint64), want[even].view(np.uint64)), omega
+        assert np.array_equal(got[~even].view(np.uint64), e[~even].view(np.uint64))
 
 
 def test_sweep(dev, kernels_golden):
