@@ -102,21 +102,27 @@ __device__ __forceinline__ bool pair_skip(PairCtl* ctl, int colour, int lp) {
   return false;
 }
 
+// Node indices fit 32 bits (grids are below 2^31 nodes).
 struct Nb {
-  size_t xm, xp, ym, yp, zm, zp;
+  uint32_t xm, xp, ym, yp, zm, zp;
 };
 
-__device__ __forceinline__ Nb neighbours(long i, long j, long k, long nx,
-                                         long ny, long nz) {
-  const size_t sy = (size_t)nz, sx = (size_t)ny * nz;
-  const size_t row = (size_t)i * sx + (size_t)j * sy;
+// The six neighbours of node p = (i, j, k) as offsets from p, with the
+// even-reflection rule at the faces (the ghost at -1 is node 1, the ghost at
+// n is node n-2; a size-1 axis uses the node itself) as selects, so the
+// interior and the faces run the same instructions.
+__device__ __forceinline__ Nb neighbours(uint32_t i, uint32_t j, uint32_t k, uint32_t nx,
+                                         uint32_t ny, uint32_t nz) {
+  const uint32_t sy = nz, sx = ny * nz;
+  const uint32_t p = (i * ny + j) * nz + k;
+  const uint32_t rx = nx > 1 ? sx : 0u, ry = ny > 1 ? sy : 0u, rz = nz > 1 ? 1u : 0u;
   Nb n;
-  n.xm = (size_t)lo_nb(i, nx) * sx + (size_t)j * sy + k;
-  n.xp = (size_t)hi_nb(i, nx) * sx + (size_t)j * sy + k;
-  n.ym = (size_t)i * sx + (size_t)lo_nb(j, ny) * sy + k;
-  n.yp = (size_t)i * sx + (size_t)hi_nb(j, ny) * sy + k;
-  n.zm = row + lo_nb(k, nz);
-  n.zp = row + hi_nb(k, nz);
+  n.xm = i > 0 ? p - sx : p + rx;
+  n.xp = i + 1 < nx ? p + sx : p - rx;
+  n.ym = j > 0 ? p - sy : p + ry;
+  n.yp = j + 1 < ny ? p + sy : p - ry;
+  n.zm = k > 0 ? p - 1 : p + rz;
+  n.zp = k + 1 < nz ? p + 1 : p - rz;
   return n;
 }
 
@@ -189,9 +195,9 @@ k_sweep(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
     const uint32_t kk = t - ij * g.div_kk.d;
     const uint32_t i = fdiv(ij, g.div_ny);
     const uint32_t j = ij - i * g.div_ny.d;
-    const long k = 2 * (long)kk + ((i + j + colour) & 1);
-    if (k < g.nz) {
-      const size_t p = ((size_t)i * g.ny + j) * g.nz + k;
+    const uint32_t k = 2 * kk + ((i + j + colour) & 1);
+    if (k < (uint32_t)g.nz) {
+      const uint32_t p = (i * (uint32_t)g.ny + j) * (uint32_t)g.nz + k;
       if (!fixed[p]) {
         const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
         double v[6];
@@ -268,9 +274,9 @@ k_sweep_rhs(double* __restrict__ e, const uint8_t* __restrict__ fixed,
     const uint32_t kk = t - ij * g.div_kk.d;
     const uint32_t i = fdiv(ij, g.div_ny);
     const uint32_t j = ij - i * g.div_ny.d;
-    const long k = 2 * (long)kk + ((i + j + colour) & 1);
-    if (k < g.nz) {
-      const size_t p = ((size_t)i * g.ny + j) * g.nz + k;
+    const uint32_t k = 2 * kk + ((i + j + colour) & 1);
+    if (k < (uint32_t)g.nz) {
+      const uint32_t p = (i * (uint32_t)g.ny + j) * (uint32_t)g.nz + k;
       if (!fixed[p]) {
         const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
         double v[6];
@@ -679,9 +685,9 @@ k_err_sweep(double* __restrict__ e, const uint8_t* __restrict__ fixed,
     const uint32_t kk = t - ij * g.div_kk.d;
     const uint32_t i = fdiv(ij, g.div_ny);
     const uint32_t j = ij - i * g.div_ny.d;
-    const long k = 2 * (long)kk + ((i + j + colour) & 1);
-    if (k < g.nz) {
-      const size_t p = ((size_t)i * g.ny + j) * g.nz + k;
+    const uint32_t k = 2 * kk + ((i + j + colour) & 1);
+    if (k < (uint32_t)g.nz) {
+      const uint32_t p = (i * (uint32_t)g.ny + j) * (uint32_t)g.nz + k;
       if (!fixed[p]) {
         const Nb n = neighbours(i, j, k, g.nx, g.ny, g.nz);
         double v[6], num, den;
