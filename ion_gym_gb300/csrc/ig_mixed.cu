@@ -240,6 +240,89 @@ __global__ void k_gs8(float* __restrict__ e, const float* __restrict__ g,
   if (q0 + 1 < H4) gs4_at<FLAT>(own, oth, gp, mp, G, c, omega, ij, i, j, 4 * (int)q0 + 4);
 }
 
+// The first Gauss-Seidel pair (omega = 1) of a cycle that starts from e = 0,
+// in one pass.  Colour 0 sees zero neighbours, so its new value is
+// (0 - g0) / 6 at free nodes and 0 at metal; colour 1 then reads those
+// colour-0 values at its six neighbours, which this thread recomputes from
+// g0 and the colour-0 mask (five float4 rows and one edge slot, the same
+// rows the separate colour-1 launch would read from e).  Every expression
+// and its order are those of gs4_at, so the result has the bits of a memset
+// and two half-sweeps, at 9 bytes per node (g, mask, both colours of e
+// written) instead of 4 + 13.  Grids with a size-1 axis use the separate
+// launches.
+__device__ __forceinline__ float zero_start_e0(float g, uint8_t m) {
+  return m ? 0.f : (0.f - g) * (1.0f / 6.0f);
+}
+__device__ __forceinline__ float4 zero_start_e0(const float* gp, const uint8_t* mp) {
+  const float4 g = ld4(gp);
+  const uchar4 m = *reinterpret_cast<const uchar4*>(mp);
+  return make_float4(zero_start_e0(g.x, m.x), zero_start_e0(g.y, m.y), zero_start_e0(g.z, m.z),
+                     zero_start_e0(g.w, m.w));
+}
+
+__global__ void __launch_bounds__(kT)
+k_gs_zero_pair(float* __restrict__ e, const float* __restrict__ g,
+               const uint8_t* __restrict__ mask, SGeo G, size_t pstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= (G.csz >> 2)) return;
+  const uint32_t ij = fdivu(t, G.dH4);
+  const int m0 = 4 * (int)(t - ij * G.dH4.d);
+  const int i = (int)fdivu(ij, G.dny);
+  const int j = (int)(ij - (uint32_t)i * G.dny.d);
+  const uint32_t base = ij * (uint32_t)G.H + m0;
+  float* e0 = e + blockIdx.y * pstride;
+  float* e1 = e0 + G.csz;
+  const float* g0 = g + blockIdx.y * pstride;
+  const float* g1 = g0 + G.csz;
+  const uint8_t* k0 = mask;
+  const uint8_t* k1 = mask + G.csz;
+  // colour 0 of this thread's slots
+  *reinterpret_cast<float4*>(e0 + base) = zero_start_e0(g0 + base, k0 + base);
+  // colour 1 of this thread's slots, from the colour-0 values around them
+  const uint32_t rxm = ((uint32_t)lo_i(i, G.nx) * G.ny + j) * G.H + m0;
+  const uint32_t rxp = ((uint32_t)hi_i(i, G.nx) * G.ny + j) * G.H + m0;
+  const uint32_t rym = ((uint32_t)i * G.ny + lo_i(j, G.ny)) * G.H + m0;
+  const uint32_t ryp = ((uint32_t)i * G.ny + hi_i(j, G.ny)) * G.H + m0;
+  const float4 xm = zero_start_e0(g0 + rxm, k0 + rxm);
+  const float4 xp = zero_start_e0(g0 + rxp, k0 + rxp);
+  const float4 ym = zero_start_e0(g0 + rym, k0 + rym);
+  const float4 yp = zero_start_e0(g0 + ryp, k0 + ryp);
+  const float4 zc = zero_start_e0(g0 + base, k0 + base);
+  const int p = (i + j + 1) & 1;
+  float z[5];
+  if (p == 0) {
+    z[0] = m0 > 0 ? zero_start_e0(g0[base - 1], k0[base - 1]) : zc.x;
+    z[1] = zc.x; z[2] = zc.y; z[3] = zc.z; z[4] = zc.w;
+  } else {
+    z[0] = zc.x; z[1] = zc.y; z[2] = zc.z; z[3] = zc.w;
+    z[4] = m0 + 4 < G.H ? zero_start_e0(g0[base + 4], k0[base + 4]) : 0.f;
+  }
+  const int utop = G.nz - 1 - p - 2 * m0;
+  const float sx[4] = {(xm.x + xp.x) + (ym.x + yp.x), (xm.y + xp.y) + (ym.y + yp.y),
+                       (xm.z + xp.z) + (ym.z + yp.z), (xm.w + xp.w) + (ym.w + yp.w)};
+  const float4 gg = ld4(g1 + base);
+  const uchar4 mk = *reinterpret_cast<const uchar4*>(k1 + base);
+  const float gv[4] = {gg.x, gg.y, gg.z, gg.w};
+  const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
+  float o[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const float q = sx[u] + (z[u] + (2 * u == utop ? z[u] : z[u + 1]));
+    o[u] = mv[u] ? 0.f : (q - gv[u]) * (1.0f / 6.0f);
+  }
+  *reinterpret_cast<float4*>(e1 + base) = make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// Number of 32-bit words that differ between a and b (a check of the fused
+// kernels against their separate launches).
+__global__ void __launch_bounds__(kT)
+k_count_diff(const uint32_t* __restrict__ a, const uint32_t* __restrict__ b, size_t n,
+             unsigned long long* bad) {
+  const size_t t = (size_t)blockIdx.x * kT + threadIdx.x;
+  const unsigned d = __syncthreads_count(t < n && a[t] != b[t]);
+  if (threadIdx.x == 0 && d) atomicAdd(bad, (unsigned long long)d);
+}
+
 // Residual r = g - A e of colour 0 only, in split layout.  After a red-black
 // Gauss-Seidel pair that ended on colour 1 the residual of colour 1 is zero
 // (each colour-1 node was just solved exactly against its neighbours), so
@@ -391,7 +474,7 @@ __global__ void __launch_bounds__(kT)
 k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
                const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
                size_t fstride) {
-  const int c = blockIdx.z;
+  const int c = blockIdx.z;  // gridDim.z = 1: colour 0 only
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= (F.csz >> 2)) return;
   const uint32_t ij = fdivu(t, F.dH4);
@@ -1011,7 +1094,16 @@ struct Session {
     cache[key] = best;
   }
 
-  void vcycle(size_t l) {
+  static bool flat(const MLevel& a) { return a.G.nx == 1 || a.G.ny == 1 || a.G.nz == 1; }
+
+  // The first pre-smoothing pair from e = 0 runs as one fused pass.
+  bool fuse_zero_pair(const MLevel& a) const {
+    return nu1 >= 1 && smooth_omega == 1.f && !flat(a);
+  }
+
+  // One cycle on level l.  zero: the level's correction starts at 0 (the
+  // cycle zeroes it, or its first Gauss-Seidel pair writes every slot).
+  void vcycle(size_t l, bool zero) {
     MLevel& a = lv[l];
     const dim3 gs(nblk(a.G.csz), B), gn(nblk(a.G.n), B);
     if (l + 1 == lv.size()) {
@@ -1019,7 +1111,15 @@ struct Session {
                                             bottom_pairs, a.pstride);
       return;
     }
-    for (int q = 0; q < nu1; q++)
+    int q0 = 0;
+    if (zero && fuse_zero_pair(a)) {
+      k_gs_zero_pair<<<dim3(nblk(a.G.csz / 4), B), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G,
+                                                              a.pstride);
+      q0 = 1;
+    } else if (zero) {
+      MK(cudaMemsetAsync(a.e.p, 0, a.pstride * B * 4, s));
+    }
+    for (int q = q0; q < nu1; q++)
       for (int c = 0; c < 2; c++) launch_gs(a, c, B, smooth_omega);
     MLevel& b = lv[l + 1];
     if (nu1 > 0 && smooth_omega == 1.f) {
@@ -1030,13 +1130,16 @@ struct Session {
       k_resid<<<gn, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p, a.pstride, a.rstride);
       k_restrict<<<dim3(nblk(b.G.n), B), kT, 0, s>>>(a.r.p, a.G, b.g.p, b.G, a.rstride, b.pstride);
     }
-    if (l + 2 < lv.size()) MK(cudaMemsetAsync(b.e.p, 0, b.pstride * B * 4, s));
-    // the coarse correction: gamma cycles on the coarse equation (the
-    // bottom is solved directly, so once is enough there)
+    // the coarse correction: gamma cycles on the coarse equation from 0
+    // (the bottom is solved directly, so once is enough there)
     const int reps = (l + 2 < lv.size()) ? gamma : 1;
-    for (int q = 0; q < reps; q++) vcycle(l + 1);
-    k_prolong_add4<<<dim3(nblk(a.G.csz / 4), B, 2), kT, 0, s>>>(b.e.p, b.G, a.e.p, a.mask.p, a.G,
-                                                            b.pstride, a.pstride);
+    for (int q = 0; q < reps; q++) vcycle(l + 1, q == 0);
+    // The first post-smoothing half-sweep (colour 1, omega 1) overwrites
+    // every free colour-1 slot without reading it, so only colour 0 takes
+    // the prolonged correction then.
+    const unsigned pcol = (nu2 >= 1 && smooth_omega == 1.f) ? 1u : 2u;
+    k_prolong_add4<<<dim3(nblk(a.G.csz / 4), B, pcol), kT, 0, s>>>(b.e.p, b.G, a.e.p, a.mask.p,
+                                                               a.G, b.pstride, a.pstride);
     // post-smoothing in the reverse colour order keeps the cycle symmetric
     for (int q = 0; q < nu2; q++)
       for (int c = 1; c >= 0; c--) launch_gs(a, c, B, smooth_omega);
@@ -1048,8 +1151,7 @@ struct Session {
     const size_t nstride = f.G.n;
     const dim3 gn(nblk(f.G.n), B);
     k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, nstride, f.pstride);
-    MK(cudaMemsetAsync(f.e.p, 0, f.pstride * B * 4, s));
-    for (int v = 0; v < vcycles; v++) vcycle(0);
+    for (int v = 0; v < vcycles; v++) vcycle(0, v == 0);
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
     k_update64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.e.p, f.G, dmax.p, nstride, f.pstride);
   }
@@ -1075,8 +1177,7 @@ struct Session {
     const unsigned nb4 = std::min(nblk(f.G.csz / 4), kCgBlocks);
     const unsigned nbd = std::min(nblk(n / 4), kCgBlocks);
     for (int it = 0; it < cg_iters; it++) {
-      MK(cudaMemsetAsync(f.e.p, 0, f.pstride * B * 4, s));
-      vcycle(0);  // z = f.e
+      vcycle(0, true);  // z = f.e
       k_cg_dot<<<dim3(nbd, B), kT, 0, s>>>(f.e.p, qb.p, part.p, f.pstride, n);
       k_cg_reduce<<<B, kT, 0, s>>>(part.p, (int)nbd, 1, scal.p, 1);
       k_cg_dir<<<gv, kT, 0, s>>>(pb.p, f.e.p, scal.p, f.pstride, n);
@@ -1112,15 +1213,21 @@ struct Session {
     MK(cudaGraphLaunch(exec, s));
   }
 
+  // kernel launches of one cycle on level l (memsets are not kernels)
+  long cycle_launches(size_t l, bool zero) const {
+    if (l + 1 == lv.size()) return 1;
+    const int reps = (l + 2 < lv.size()) ? gamma : 1;
+    long n = 2 * (nu1 + nu2) + 3;
+    if (zero && fuse_zero_pair(lv[l])) n -= 1;
+    for (int q = 0; q < reps; q++) n += cycle_launches(l + 1, q == 0);
+    return n;
+  }
+
   long launches_per_step() const {
-    // launches of one cycle at level l, recursively
-    std::vector<long> c(lv.size(), 1);
-    for (int l = (int)lv.size() - 2; l >= 0; l--) {
-      const int reps = (l + 2 < (int)lv.size()) ? gamma : 1;
-      c[l] = 2 * (nu1 + nu2) + 3 + reps * c[l + 1];
-    }
-    if (method == 1) return 2 + cg_iters * (c[0] + 6);
-    return 2 + c[0] * vcycles;
+    if (method == 1) return 2 + cg_iters * (cycle_launches(0, true) + 6);
+    long n = 2;
+    for (int v = 0; v < vcycles; v++) n += cycle_launches(0, v == 0);
+    return n;
   }
 };
 
@@ -1278,6 +1385,48 @@ int ig_mixed_time_gs(void* handle, int n_problems, int pairs, double* ms_per_lau
     // right-hand side (4) and mask (1), write e (4); per node of the other
     // colour read e once (4)
     if (bytes_per_launch) *bytes_per_launch = (double)n_problems * (double)S->d.n() * 6.5;
+    return (int)IG_OK;
+  } catch (int code) {
+    return code;
+  }
+}
+
+int ig_mixed_check_zero_pair(void* handle, int n_problems, long long* mismatches) {
+  set_last_error("");
+  Session* S = static_cast<Session*>(handle);
+  if (!S || !mismatches || n_problems < 1 || n_problems > S->bmax || S->method != 1 ||
+      !S->qb.p) {
+    set_last_error("bad session (flexible-CG sessions only) or problem count");
+    return IG_BAD_ARG;
+  }
+  try {
+    if (!S->gs_tuned) S->tune_gs(n_problems);
+    Buf<unsigned long long> bad;
+    bad.alloc(1, S->s);
+    MK(cudaMemsetAsync(bad.p, 0, 8, S->s));
+    long launches = 0;
+    for (size_t l = 0; l + 1 < S->lv.size(); l++) {
+      MLevel& a = S->lv[l];
+      if (Session::flat(a)) continue;
+      const size_t bytes = a.pstride * n_problems * 4;
+      // a stand-in correction left over from an earlier cycle: both ways
+      // must overwrite all of it
+      MK(cudaMemsetAsync(a.e.p, 0x7f, bytes, S->s));
+      k_gs_zero_pair<<<dim3(nblk(a.G.csz / 4), n_problems), kT, 0, S->s>>>(
+          a.e.p, a.g.p, a.mask.p, a.G, a.pstride);
+      MK(cudaMemcpyAsync(S->qb.p, a.e.p, bytes, cudaMemcpyDeviceToDevice, S->s));
+      MK(cudaMemsetAsync(a.e.p, 0, bytes, S->s));
+      for (int c = 0; c < 2; c++) S->launch_gs(a, c, n_problems, 1.f);
+      k_count_diff<<<dim3(nblk((uint32_t)(a.pstride * n_problems)), 1), kT, 0, S->s>>>(
+          reinterpret_cast<const uint32_t*>(a.e.p), reinterpret_cast<const uint32_t*>(S->qb.p),
+          a.pstride * n_problems, bad.p);
+      launches += 4;
+    }
+    unsigned long long h = 0;
+    MK(cudaMemcpyAsync(&h, bad.p, 8, cudaMemcpyDeviceToHost, S->s));
+    MK(cudaStreamSynchronize(S->s));
+    g_mixed_launches.fetch_add(launches);
+    *mismatches = (long long)h;
     return (int)IG_OK;
   } catch (int code) {
     return code;

@@ -71,3 +71,26 @@ def test_mixed_only_and_superposition():
     part = solve_bases_mixed(masks, v_basis=V, accuracy=ACC, only={2, 3})
     assert sorted(part) == [2, 3]
     assert np.abs(part[2] - got[2]).max() <= 2 * ACC * V
+
+
+@pytest.mark.parametrize("shape,seed", [((41, 37, 45), 1), ((33, 20, 18), 2)])
+def test_fused_zero_start_pair_is_bit_identical(shape, seed):
+    """The fused first Gauss-Seidel pair of a cycle from a zero correction
+    (one pass over g and the mask) writes the bits of a zeroed correction
+    followed by the two separate half-sweeps, on every multigrid level, for
+    odd and even z extents (both row parities at the z faces)."""
+    import ctypes
+    from ion_gym_gb300 import _lib
+    from ion_gym_gb300.physics.mixed import MixedSession
+    masks = _deck(shape, seed)
+    metal = np.zeros(shape, bool)
+    for m in masks.values():
+        metal |= m
+    rings = [masks[i] for i in sorted(masks)]
+    with MixedSession(metal, len(rings)) as s:
+        s.solve_bases(rings, V, ACC)
+        bad = ctypes.c_longlong(-1)
+        st = _lib.lib().ig_mixed_check_zero_pair(s._h, len(rings),
+                                                 ctypes.byref(bad))
+        _lib.check(st, "ig_mixed_check_zero_pair")
+    assert bad.value == 0
