@@ -191,15 +191,19 @@ void ig_mixed_close(void *handle);
  * bytes (6.5 B per node and problem). */
 int ig_mixed_time_gs(void *handle, int n_problems, int pairs,
                      double *ms_per_launch, double *bytes_per_launch);
-/* Checks the fused first Gauss-Seidel pair of a cycle that starts from a
- * zero correction (one pass over g and the mask) against a zeroed correction
- * followed by the two separate half-sweeps, on every multigrid level of the
- * session (right-hand sides as the last solve left them): *mismatches = the
- * number of 32-bit words that differ (0 when the two are bit-identical).
+/* Checks the fused kernels of the mixed path against the separate launches
+ * they replace, on the state the session's last solve left (right-hand
+ * sides, corrections, direction): mismatches[0] = the first Gauss-Seidel
+ * pair from a zero correction vs a zeroed correction and two half-sweeps,
+ * [1] = the float4 colour-0 residual vs the per-slot one, [2] = the
+ * windowed prolongation vs the per-node gather, [3] = the direction update
+ * fused into the operator apply vs the two kernels (direction, L p and the
+ * block partials of the inner products) -- each the number of 32-bit words
+ * that differ over every multigrid level, 0 when bit-identical.
  * Flexible-CG sessions only; no reference counterpart (a self-check of this
  * library's kernel fusion). */
-int ig_mixed_check_zero_pair(void *handle, int n_problems,
-                             long long *mismatches);
+int ig_mixed_check_fused(void *handle, int n_problems,
+                         long long mismatches[4]);
 
 /* ig_cascadic_relres for callers that cannot allocate device memory (no
  * counterpart in the reference).  Some callers may not call cudaMalloc, or

@@ -113,6 +113,56 @@ __device__ __forceinline__ float4 ld4(const float* p) {
   return *reinterpret_cast<const float4*>(p);
 }
 
+// Neighbour sums of the four slots m0..m0+3 (k parity p) of row (i, j),
+// read from the other colour's array `oth` (grids with no size-1 axis):
+// 16-byte loads of the x/y neighbour rows and of the row's own other-colour
+// slots.  The z neighbours of slot m (node k = 2m + p) are slots m-1+p and
+// m+p of the other colour's row; node 0 reflects k-1 to k+1 (slot 0), node
+// nz-1 reflects k+1 to k-1.  The slot past the row's end (p = 1, last
+// group) only feeds unused slots, whose results are never kept.  Sum order:
+// ((xm + xp) + (ym + yp)) + (zm + zp).
+// Values of the other colour's array: plain loads.
+struct PlainLd {
+  const float* __restrict__ a;
+  __device__ __forceinline__ float4 v4(uint32_t o) const { return ld4(a + o); }
+  __device__ __forceinline__ float v1(uint32_t o) const { return a[o]; }
+};
+// Values of the new CG direction z + beta p, formed where they are read
+// (the expression k_cg_dir stores).
+struct DirLd {
+  const float* __restrict__ z;
+  const float* __restrict__ p;
+  float b;
+  __device__ __forceinline__ float4 v4(uint32_t o) const {
+    const float4 zz = ld4(z + o), pp = ld4(p + o);
+    return make_float4(zz.x + b * pp.x, zz.y + b * pp.y, zz.z + b * pp.z, zz.w + b * pp.w);
+  }
+  __device__ __forceinline__ float v1(uint32_t o) const { return z[o] + b * p[o]; }
+};
+
+template <class L>
+__device__ __forceinline__ void nbr4(const L& oth, const SGeo& G, int i, int j, int m0, int p,
+                                     uint32_t base, float q[4]) {
+  const float4 xm = oth.v4(((uint32_t)lo_i(i, G.nx) * G.ny + j) * G.H + m0);
+  const float4 xp = oth.v4(((uint32_t)hi_i(i, G.nx) * G.ny + j) * G.H + m0);
+  const float4 ym = oth.v4(((uint32_t)i * G.ny + lo_i(j, G.ny)) * G.H + m0);
+  const float4 yp = oth.v4(((uint32_t)i * G.ny + hi_i(j, G.ny)) * G.H + m0);
+  const float4 zc = oth.v4(base);
+  float z[5];
+  if (p == 0) {
+    z[0] = m0 > 0 ? oth.v1(base - 1) : zc.x;
+    z[1] = zc.x; z[2] = zc.y; z[3] = zc.z; z[4] = zc.w;
+  } else {
+    z[0] = zc.x; z[1] = zc.y; z[2] = zc.z; z[3] = zc.w;
+    z[4] = m0 + 4 < G.H ? oth.v1(base + 4) : 0.f;
+  }
+  const int utop = G.nz - 1 - p - 2 * m0;  // 2u == utop: node nz-1
+  const float sx[4] = {(xm.x + xp.x) + (ym.x + yp.x), (xm.y + xp.y) + (ym.y + yp.y),
+                       (xm.z + xp.z) + (ym.z + yp.z), (xm.w + xp.w) + (ym.w + yp.w)};
+#pragma unroll
+  for (int u = 0; u < 4; u++) q[u] = sx[u] + (z[u] + (2 * u == utop ? z[u] : z[u + 1]));
+}
+
 // One float4 group (slots m0..m0+3 of colour c, row ij) of the update.
 // FLAT: the grid has a size-1 axis (per-slot neighbour sums).
 template <bool FLAT>
@@ -130,30 +180,7 @@ __device__ __forceinline__ void gs4_at(float* __restrict__ own, const float* __r
   // faces included, so no warp diverges into a per-slot path at the ends of
   // its rows.
   if (!FLAT) {
-    const float4 xm = ld4(oth + ((uint32_t)lo_i(i, G.nx) * G.ny + j) * G.H + m0);
-    const float4 xp = ld4(oth + ((uint32_t)hi_i(i, G.nx) * G.ny + j) * G.H + m0);
-    const float4 ym = ld4(oth + ((uint32_t)i * G.ny + lo_i(j, G.ny)) * G.H + m0);
-    const float4 yp = ld4(oth + ((uint32_t)i * G.ny + hi_i(j, G.ny)) * G.H + m0);
-    const float4 zc = ld4(oth + base);
-    // z neighbours of slot m (node k = 2m + p): k-1 is slot m-1+p and k+1
-    // slot m+p of the other colour's row.  Node 0 reflects k-1 to k+1
-    // (slot 0); node nz-1 reflects k+1 to k-1.  The slot past the row's end
-    // (p = 1, last group) only feeds unused slots, which are never written.
-    float z[5];
-    if (p == 0) {
-      z[0] = m0 > 0 ? oth[base - 1] : zc.x;
-      z[1] = zc.x; z[2] = zc.y; z[3] = zc.z; z[4] = zc.w;
-    } else {
-      z[0] = zc.x; z[1] = zc.y; z[2] = zc.z; z[3] = zc.w;
-      z[4] = m0 + 4 < G.H ? oth[base + 4] : 0.f;
-    }
-    const int utop = G.nz - 1 - p - 2 * m0;  // 2u == utop: node nz-1
-    const float4 s4 = make_float4((xm.x + xp.x) + (ym.x + yp.x), (xm.y + xp.y) + (ym.y + yp.y),
-                                  (xm.z + xp.z) + (ym.z + yp.z), (xm.w + xp.w) + (ym.w + yp.w));
-    const float sx[4] = {s4.x, s4.y, s4.z, s4.w};
-#pragma unroll
-    for (int u = 0; u < 4; u++)
-      q[u] = sx[u] + (z[u] + (2 * u == utop ? z[u] : z[u + 1]));
+    nbr4(PlainLd{oth}, G, i, j, m0, p, base, q);
   } else {
 #pragma unroll
     for (int u = 0; u < 4; u++) {
@@ -347,6 +374,41 @@ k_resid0(const float* __restrict__ e, const float* __restrict__ g,
   r[blockIdx.y * (size_t)G.csz + t] = out;
 }
 
+// k_resid0 over float4 groups (grids with no size-1 axis): the same
+// expressions per slot, 16-byte loads of the colour-1 neighbour rows, one
+// float4 store of r.
+__global__ void __launch_bounds__(kT)
+k_resid0_4(const float* __restrict__ e, const float* __restrict__ g,
+           const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ r,
+           size_t pstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= (G.csz >> 2)) return;
+  const uint32_t ij = fdivu(t, G.dH4);
+  const int m0 = 4 * (int)(t - ij * G.dH4.d);
+  const int i = (int)fdivu(ij, G.dny);
+  const int j = (int)(ij - (uint32_t)i * G.dny.d);
+  const uint32_t base = ij * (uint32_t)G.H + m0;
+  float4* out = reinterpret_cast<float4*>(r + blockIdx.y * (size_t)G.csz + base);
+  const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + base);
+  if (mk.x & mk.y & mk.z & mk.w) {
+    *out = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const float* eb = e + blockIdx.y * pstride;
+  float q[4];
+  nbr4(PlainLd{eb + G.csz}, G, i, j, m0, (i + j) & 1, base, q);
+  const float4 ev = ld4(eb + base), gg = ld4(g + blockIdx.y * pstride + base);
+  const float es[4] = {ev.x, ev.y, ev.z, ev.w}, gv[4] = {gg.x, gg.y, gg.z, gg.w};
+  const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
+  float o[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const float a = q[u] - 6.0f * es[u];
+    o[u] = mv[u] ? 0.f : gv[u] - a;
+  }
+  *out = make_float4(o[0], o[1], o[2], o[3]);
+}
+
 // 4 x full weighting when only colour 0 of the fine residual is nonzero:
 // around a coarse node (fine centre 2c, colour 0) the colour-0 points are
 // the centre (weight 1) and the 12 edge neighbours (weight 1/4); the faces
@@ -471,7 +533,7 @@ __device__ __forceinline__ float cget(const float* eb, const SGeo& C, int i, int
 // thread) and the fine correction is read and written as one float4.  The
 // per-node sum is formed in x, y, z order.
 __global__ void __launch_bounds__(kT)
-k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
+k_prolong_add4_gather(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
                const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
                size_t fstride) {
   const int c = blockIdx.z;  // gridDim.z = 1: colour 0 only
@@ -521,6 +583,81 @@ k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
   v.y += add[1];
   v.z += add[2];
   v.w += add[3];
+  *out = v;
+}
+
+// The same correction with the coarse values fetched once per thread: the
+// fine slots m0..m0+3 of one colour row sit at coarse z positions m0 + u
+// (+1/2 for odd k), so all four read coarse nodes kc = m0 .. m0+4 of at most
+// four coarse rows -- five values per row, three from one colour array and
+// two from the other (kc alternates colour; slot kc >> 1) -- instead of
+// locating every coarse node separately.  Per fine node the weights, the
+// skipped zero weights and the x, y, z summation order are those of
+// k_prolong_add4_gather, so the results are the same bits.  Needs every
+// axis of both grids at least 2 nodes long.
+__global__ void __launch_bounds__(kT)
+k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
+               const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
+               size_t fstride) {
+  const int c = blockIdx.z;  // gridDim.z = 1: colour 0 only
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= (F.csz >> 2)) return;
+  const uint32_t ij = fdivu(t, F.dH4);
+  const int m0 = 4 * (int)(t - ij * F.dH4.d);
+  const int i = (int)fdivu(ij, F.dny);
+  const int j = (int)(ij - (uint32_t)i * F.dny.d);
+  const int pc = (i + j + c) & 1;
+  const uint32_t base = ij * (uint32_t)F.H + m0;
+  const uchar4 mk = *reinterpret_cast<const uchar4*>(maskf + (size_t)c * F.csz + base);
+  if (mk.x & mk.y & mk.z & mk.w) return;  // metal or unused: nothing to add
+  const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
+  const float* eb = ec + blockIdx.y * cstride;
+  const LerpF x = pa(i, C.nx), y = pa(j, C.ny);
+  int xi[2], yi[2];
+  float xw[2], yw[2];
+  int nxw = 0, nyw = 0;
+  if (x.t != 1.f) { xi[nxw] = x.a0; xw[nxw++] = 1.f - x.t; }
+  if (x.t != 0.f) { xi[nxw] = x.a1; xw[nxw++] = x.t; }
+  if (y.t != 1.f) { yi[nyw] = y.a0; yw[nyw++] = 1.f - y.t; }
+  if (y.t != 0.f) { yi[nyw] = y.a1; yw[nyw++] = y.t; }
+  // z weights of the four fine nodes as offsets v = kc - m0 into the window
+  int zv[4][2];
+  float zw[4][2];
+  int nzw[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const LerpF z = pa(2 * (m0 + u) + pc, C.nz);
+    nzw[u] = 0;
+    if (z.t != 1.f) { zv[u][nzw[u]] = z.a0 - m0; zw[u][nzw[u]++] = 1.f - z.t; }
+    if (z.t != 0.f) { zv[u][nzw[u]] = z.a1 - m0; zw[u][nzw[u]++] = z.t; }
+  }
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int a = 0; a < nxw; a++)
+    for (int b = 0; b < nyw; b++) {
+      const uint32_t row = ((uint32_t)xi[a] * C.ny + yi[b]) * C.H + (m0 >> 1);
+      const int ca = (xi[a] + yi[b] + m0) & 1;
+      const float* A = eb + (size_t)ca * C.csz + row;
+      const float* Bc = eb + (size_t)(1 - ca) * C.csz + row;
+      float cv[5];
+      cv[0] = A[0];
+      cv[1] = m0 + 1 < C.nz ? Bc[0] : 0.f;
+      cv[2] = m0 + 2 < C.nz ? A[1] : 0.f;
+      cv[3] = m0 + 3 < C.nz ? Bc[1] : 0.f;
+      cv[4] = m0 + 4 < C.nz ? A[2] : 0.f;
+      const float w = xw[a] * yw[b];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        float zs = 0.f;
+        for (int q = 0; q < nzw[u]; q++) zs += zw[u][q] * cv[zv[u][q]];
+        acc[u] += w * zs;
+      }
+    }
+  float4* out = reinterpret_cast<float4*>(ef + fstride * blockIdx.y + (size_t)c * F.csz + base);
+  float4 v = *out;
+  v.x += mv[0] ? 0.f : acc[0];
+  v.y += mv[1] ? 0.f : acc[1];
+  v.z += mv[2] ? 0.f : acc[2];
+  v.w += mv[3] ? 0.f : acc[3];
   *out = v;
 }
 
@@ -766,6 +903,64 @@ k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
   }
 }
 
+// k_cg_dir and k_cg_matvec in one pass (grids with no size-1 axis): the new
+// direction p = z + beta p_old is formed where it is read -- at the thread's
+// own slots (stored to pn) and at their six neighbours -- so z and p_old are
+// read once and p is written once.  p_old and pn are different arrays (a
+// thread of one colour reads the other colour's p_old while that colour's
+// threads store theirs).  Same expressions as the two kernels, same bits.
+__global__ void __launch_bounds__(kT)
+k_cg_matvec_dir(const float* __restrict__ z, const float* __restrict__ po,
+                float* __restrict__ pn, const double* __restrict__ scal,
+                const float* __restrict__ g, const uint8_t* __restrict__ mask, SGeo G,
+                float* __restrict__ q, double* __restrict__ part, size_t pstride) {
+  __shared__ double sh[kT / 32];
+  const int c = blockIdx.z;
+  const uint32_t nq = G.csz >> 2;
+  const float b = (float)scal[4 * blockIdx.y + 2];
+  KSum spq, spg;
+  const size_t own = blockIdx.y * pstride + (size_t)c * G.csz;
+  const size_t oth = blockIdx.y * pstride + (size_t)(1 - c) * G.csz;
+  const DirLd on{z + oth, po + oth, b};
+  for (uint32_t t = blockIdx.x * kT + threadIdx.x; t < nq; t += gridDim.x * kT) {
+    const uint32_t ij = fdivu(t, G.dH4);
+    const int m0 = 4 * (int)(t - ij * G.dH4.d);
+    const int i = (int)fdivu(ij, G.dny);
+    const int j = (int)(ij - (uint32_t)i * G.dny.d);
+    const int pc = (i + j + c) & 1;
+    const uint32_t base = ij * (uint32_t)G.H + m0;
+    const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + (size_t)c * G.csz + base);
+    const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
+    const float4 pv = DirLd{z + own, po + own, b}.v4(base);
+    *reinterpret_cast<float4*>(pn + own + base) = pv;
+    const float4 gv = ld4(g + own + base);
+    const float pp[4] = {pv.x, pv.y, pv.z, pv.w};
+    const float gg[4] = {gv.x, gv.y, gv.z, gv.w};
+    float out[4] = {0.f, 0.f, 0.f, 0.f};
+    if (!(mk.x & mk.y & mk.z & mk.w)) {
+      float nb[4];
+      nbr4(on, G, i, j, m0, pc, base, nb);
+#pragma unroll
+      for (int u = 0; u < 4; u++)
+        if (!mv[u]) out[u] = 6.0f * pp[u] - nb[u];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      spq.add(pp[u] * out[u]);
+      spg.add(pp[u] * gg[u]);
+    }
+    *reinterpret_cast<float4*>(q + own + base) = make_float4(out[0], out[1], out[2], out[3]);
+  }
+  const double a = block_sum_d(spq.value(), sh);
+  __syncthreads();
+  const double bb = block_sum_d(spg.value(), sh);
+  if (threadIdx.x == 0) {
+    const size_t slot = ((size_t)blockIdx.y * 2 + c) * gridDim.x + blockIdx.x;
+    part[2 * slot] = a;
+    part[2 * slot + 1] = bb;
+  }
+}
+
 // block partials of <z, q>: grid-stride over float4 groups, kCgBlocks
 // blocks per problem
 __global__ void __launch_bounds__(kT)
@@ -897,8 +1092,10 @@ size_t session_bytes(Dims fine, int bmax) {
   size_t b = fine.n() * (1 + 8 * (size_t)bmax + (size_t)bmax);  // mask, phi, masks/values staging
   Dims d = fine;
   while (true) {
-    const size_t csz = (size_t)d.nx * d.ny * ((d.nz + 1) / 2);
+    const size_t csz = (size_t)d.nx * d.ny * (size_t)((((d.nz + 1) / 2) + 3) & ~3L);
     b += d.n() + 2 * csz + 2 * (2 * csz * 4 * (size_t)bmax);
+    // level 0: the flexible CG's correction, two direction buffers and L p
+    if (d.n() == fine.n()) b += 4 * (2 * csz * 4 * (size_t)bmax);
     if (is_bottom(d)) break;
     b += d.n() * 4 * (size_t)bmax;
     d = coarse_of(d);
@@ -932,6 +1129,7 @@ struct Session {
   // flexible CG state (level 0, split FP32): correction x, direction p,
   // q = L p; dot-product partials and per-problem scalars
   Buf<float> xb, pb, qb;
+  Buf<float> pb2;  // the other buffer of the direction (fused dir + matvec)
   Buf<double> part, scal;
   int method = 1;            // 0: defect correction with `vcycles` cycles,
                              // 1: flexible CG preconditioned by one cycle
@@ -955,6 +1153,7 @@ struct Session {
     dmax.release();
     xb.release();
     pb.release();
+    pb2.release();
     qb.release();
     part.release();
     scal.release();
@@ -1001,6 +1200,7 @@ struct Session {
       const size_t ps = lv[0].pstride * bmax;
       xb.alloc(ps, s);
       pb.alloc(ps, s);
+      if (!flat(lv[0])) pb2.alloc(ps, s);
       qb.alloc(ps, s);
       const size_t nb4 = nblk(lv[0].G.csz / 4), nbn = nblk((uint32_t)lv[0].pstride);
       part.alloc(std::max(4 * nb4, nbn) * bmax, s);
@@ -1095,6 +1295,21 @@ struct Session {
   }
 
   static bool flat(const MLevel& a) { return a.G.nx == 1 || a.G.ny == 1 || a.G.nz == 1; }
+  static bool two_or_more(const MLevel& a) { return a.G.nx > 1 && a.G.ny > 1 && a.G.nz > 1; }
+
+  // fine a.e += trilinear(coarse b.e) for colours 0 .. ncol-1
+  void launch_prolong(MLevel& b, MLevel& a, int nb, unsigned ncol) {
+    const dim3 grid(nblk(a.G.csz / 4), nb, ncol);
+    if (two_or_more(a) && two_or_more(b))
+      k_prolong_add4<<<grid, kT, 0, s>>>(b.e.p, b.G, a.e.p, a.mask.p, a.G, b.pstride, a.pstride);
+    else
+      k_prolong_add4_gather<<<grid, kT, 0, s>>>(b.e.p, b.G, a.e.p, a.mask.p, a.G, b.pstride,
+                                                a.pstride);
+  }
+
+  // the direction update and the operator apply fuse on grids with no
+  // size-1 axis (two direction buffers)
+  bool fuse_dir() const { return pb2.p != nullptr; }
 
   // The first pre-smoothing pair from e = 0 runs as one fused pass.
   bool fuse_zero_pair(const MLevel& a) const {
@@ -1124,7 +1339,11 @@ struct Session {
     MLevel& b = lv[l + 1];
     if (nu1 > 0 && smooth_omega == 1.f) {
       // Gauss-Seidel ended on colour 1: its residual is zero
-      k_resid0<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p, a.pstride);
+      if (flat(a))
+        k_resid0<<<gs, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p, a.pstride);
+      else
+        k_resid0_4<<<dim3(nblk(a.G.csz / 4), B), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G,
+                                                            a.r.p, a.pstride);
       k_restrict0<<<dim3(nblk(b.G.n), B), kT, 0, s>>>(a.r.p, a.G, b.g.p, b.G, b.pstride);
     } else {
       k_resid<<<gn, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p, a.pstride, a.rstride);
@@ -1138,8 +1357,7 @@ struct Session {
     // every free colour-1 slot without reading it, so only colour 0 takes
     // the prolonged correction then.
     const unsigned pcol = (nu2 >= 1 && smooth_omega == 1.f) ? 1u : 2u;
-    k_prolong_add4<<<dim3(nblk(a.G.csz / 4), B, pcol), kT, 0, s>>>(b.e.p, b.G, a.e.p, a.mask.p,
-                                                               a.G, b.pstride, a.pstride);
+    launch_prolong(b, a, B, pcol);
     // post-smoothing in the reverse colour order keeps the cycle symmetric
     for (int q = 0; q < nu2; q++)
       for (int c = 1; c >= 0; c--) launch_gs(a, c, B, smooth_omega);
@@ -1176,16 +1394,27 @@ struct Session {
     const dim3 gv(nblk(n), B);
     const unsigned nb4 = std::min(nblk(f.G.csz / 4), kCgBlocks);
     const unsigned nbd = std::min(nblk(n / 4), kCgBlocks);
+    float* pcur = pb.p;
+    float* pnext = pb2.p;
     for (int it = 0; it < cg_iters; it++) {
       vcycle(0, true);  // z = f.e
       k_cg_dot<<<dim3(nbd, B), kT, 0, s>>>(f.e.p, qb.p, part.p, f.pstride, n);
       k_cg_reduce<<<B, kT, 0, s>>>(part.p, (int)nbd, 1, scal.p, 1);
-      k_cg_dir<<<gv, kT, 0, s>>>(pb.p, f.e.p, scal.p, f.pstride, n);
-      k_cg_matvec<<<dim3(nb4, B, 2), kT, 0, s>>>(pb.p, f.g.p, f.mask.p, f.G, qb.p, part.p,
-                                                f.pstride);
+      if (fuse_dir()) {
+        k_cg_matvec_dir<<<dim3(nb4, B, 2), kT, 0, s>>>(f.e.p, pcur, pnext, scal.p, f.g.p,
+                                                      f.mask.p, f.G, qb.p, part.p, f.pstride);
+        std::swap(pcur, pnext);
+      } else {
+        k_cg_dir<<<gv, kT, 0, s>>>(pcur, f.e.p, scal.p, f.pstride, n);
+        k_cg_matvec<<<dim3(nb4, B, 2), kT, 0, s>>>(pcur, f.g.p, f.mask.p, f.G, qb.p, part.p,
+                                                  f.pstride);
+      }
       k_cg_reduce<<<B, kT, 0, s>>>(part.p, 2 * (int)nb4, 2, scal.p, 0);
-      k_cg_update<<<gv, kT, 0, s>>>(xb.p, f.g.p, pb.p, qb.p, scal.p, f.pstride, n);
+      k_cg_update<<<gv, kT, 0, s>>>(xb.p, f.g.p, pcur, qb.p, scal.p, f.pstride, n);
     }
+    // the next step (a replay of this graph) starts from pb
+    if (pcur != pb.p)
+      MK(cudaMemcpyAsync(pb.p, pcur, f.pstride * B * 4, cudaMemcpyDeviceToDevice, s));
     const dim3 gn(nblk(f.G.n), B);
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
     k_update64<<<gn, kT, 0, s>>>(phi.p, fixed.p, xb.p, f.G, dmax.p, f.G.n, f.pstride);
@@ -1224,7 +1453,7 @@ struct Session {
   }
 
   long launches_per_step() const {
-    if (method == 1) return 2 + cg_iters * (cycle_launches(0, true) + 6);
+    if (method == 1) return 2 + cg_iters * (cycle_launches(0, true) + (fuse_dir() ? 5 : 6));
     long n = 2;
     for (int v = 0; v < vcycles; v++) n += cycle_launches(0, v == 0);
     return n;
@@ -1391,7 +1620,7 @@ int ig_mixed_time_gs(void* handle, int n_problems, int pairs, double* ms_per_lau
   }
 }
 
-int ig_mixed_check_zero_pair(void* handle, int n_problems, long long* mismatches) {
+int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[4]) {
   set_last_error("");
   Session* S = static_cast<Session*>(handle);
   if (!S || !mismatches || n_problems < 1 || n_problems > S->bmax || S->method != 1 ||
@@ -1401,32 +1630,79 @@ int ig_mixed_check_zero_pair(void* handle, int n_problems, long long* mismatches
   }
   try {
     if (!S->gs_tuned) S->tune_gs(n_problems);
+    const int B = n_problems;
+    cudaStream_t s = S->s;
     Buf<unsigned long long> bad;
-    bad.alloc(1, S->s);
-    MK(cudaMemsetAsync(bad.p, 0, 8, S->s));
+    bad.alloc(4, s);
+    MK(cudaMemsetAsync(bad.p, 0, 32, s));
     long launches = 0;
+    auto diff = [&](const void* a, const void* b, size_t words, int slot) {
+      k_count_diff<<<dim3((unsigned)((words + kT - 1) / kT), 1), kT, 0, s>>>(
+          static_cast<const uint32_t*>(a), static_cast<const uint32_t*>(b), words, bad.p + slot);
+      launches++;
+    };
+    float* scrA = S->xb.p;  // the CG vectors are scratch between solves
+    float* scrB = S->qb.p;
     for (size_t l = 0; l + 1 < S->lv.size(); l++) {
       MLevel& a = S->lv[l];
+      MLevel& b = S->lv[l + 1];
+      const size_t words = a.pstride * B;
+      const size_t bytes = words * 4;
+      // the prolongation, both colours, on the corrections the solve left
+      MK(cudaMemcpyAsync(scrA, a.e.p, bytes, cudaMemcpyDeviceToDevice, s));
+      S->launch_prolong(b, a, B, 2);
+      MK(cudaMemcpyAsync(scrB, a.e.p, bytes, cudaMemcpyDeviceToDevice, s));
+      MK(cudaMemcpyAsync(a.e.p, scrA, bytes, cudaMemcpyDeviceToDevice, s));
+      k_prolong_add4_gather<<<dim3(nblk(a.G.csz / 4), B, 2), kT, 0, s>>>(
+          b.e.p, b.G, a.e.p, a.mask.p, a.G, b.pstride, a.pstride);
+      diff(a.e.p, scrB, words, 2);
+      launches += 2;
       if (Session::flat(a)) continue;
-      const size_t bytes = a.pstride * n_problems * 4;
-      // a stand-in correction left over from an earlier cycle: both ways
-      // must overwrite all of it
-      MK(cudaMemsetAsync(a.e.p, 0x7f, bytes, S->s));
-      k_gs_zero_pair<<<dim3(nblk(a.G.csz / 4), n_problems), kT, 0, S->s>>>(
-          a.e.p, a.g.p, a.mask.p, a.G, a.pstride);
-      MK(cudaMemcpyAsync(S->qb.p, a.e.p, bytes, cudaMemcpyDeviceToDevice, S->s));
-      MK(cudaMemsetAsync(a.e.p, 0, bytes, S->s));
-      for (int c = 0; c < 2; c++) S->launch_gs(a, c, n_problems, 1.f);
-      k_count_diff<<<dim3(nblk((uint32_t)(a.pstride * n_problems)), 1), kT, 0, S->s>>>(
-          reinterpret_cast<const uint32_t*>(a.e.p), reinterpret_cast<const uint32_t*>(S->qb.p),
-          a.pstride * n_problems, bad.p);
-      launches += 4;
+      // the colour-0 residual after a Gauss-Seidel pair
+      k_resid0<<<dim3(nblk(a.G.csz), B), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p,
+                                                    a.pstride);
+      MK(cudaMemcpyAsync(scrA, a.r.p, (size_t)a.G.csz * B * 4, cudaMemcpyDeviceToDevice, s));
+      k_resid0_4<<<dim3(nblk(a.G.csz / 4), B), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p,
+                                                          a.pstride);
+      diff(a.r.p, scrA, (size_t)a.G.csz * B, 1);
+      launches += 2;
+      // the fused first pair from a zero correction (a stand-in correction
+      // left over from an earlier cycle: both ways must overwrite all of it)
+      MK(cudaMemsetAsync(a.e.p, 0x7f, bytes, s));
+      k_gs_zero_pair<<<dim3(nblk(a.G.csz / 4), B), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G,
+                                                              a.pstride);
+      MK(cudaMemcpyAsync(scrA, a.e.p, bytes, cudaMemcpyDeviceToDevice, s));
+      MK(cudaMemsetAsync(a.e.p, 0, bytes, s));
+      for (int c = 0; c < 2; c++) S->launch_gs(a, c, B, 1.f);
+      diff(a.e.p, scrA, words, 0);
+      launches += 3;
     }
-    unsigned long long h = 0;
-    MK(cudaMemcpyAsync(&h, bad.p, 8, cudaMemcpyDeviceToHost, S->s));
-    MK(cudaStreamSynchronize(S->s));
+    // the fused direction update + operator apply on level 0, from the
+    // direction, correction and beta the solve left
+    if (S->fuse_dir()) {
+      MLevel& f = S->lv[0];
+      const size_t words = f.pstride * B;
+      const unsigned nb4 = std::min(nblk(f.G.csz / 4), kCgBlocks);
+      const size_t nparts = 2 * (size_t)B * 2 * nb4;
+      Buf<double> part2;
+      part2.alloc(nparts, s);
+      k_cg_matvec_dir<<<dim3(nb4, B, 2), kT, 0, s>>>(f.e.p, S->pb.p, S->pb2.p, S->scal.p,
+                                                    f.g.p, f.mask.p, f.G, scrB, part2.p,
+                                                    f.pstride);
+      k_cg_dir<<<dim3(nblk((uint32_t)f.pstride), B), kT, 0, s>>>(S->pb.p, f.e.p, S->scal.p,
+                                                                 f.pstride, (uint32_t)f.pstride);
+      k_cg_matvec<<<dim3(nb4, B, 2), kT, 0, s>>>(S->pb.p, f.g.p, f.mask.p, f.G, scrA,
+                                                S->part.p, f.pstride);
+      diff(S->pb.p, S->pb2.p, words, 3);
+      diff(scrA, scrB, words, 3);
+      diff(S->part.p, part2.p, 2 * nparts, 3);
+      launches += 3;
+    }
+    unsigned long long h[4] = {0, 0, 0, 0};
+    MK(cudaMemcpyAsync(h, bad.p, 32, cudaMemcpyDeviceToHost, s));
+    MK(cudaStreamSynchronize(s));
     g_mixed_launches.fetch_add(launches);
-    *mismatches = (long long)h;
+    for (int q = 0; q < 4; q++) mismatches[q] = (long long)h[q];
     return (int)IG_OK;
   } catch (int code) {
     return code;

@@ -73,12 +73,16 @@ def test_mixed_only_and_superposition():
     assert np.abs(part[2] - got[2]).max() <= 2 * ACC * V
 
 
-@pytest.mark.parametrize("shape,seed", [((41, 37, 45), 1), ((33, 20, 18), 2)])
-def test_fused_zero_start_pair_is_bit_identical(shape, seed):
-    """The fused first Gauss-Seidel pair of a cycle from a zero correction
-    (one pass over g and the mask) writes the bits of a zeroed correction
-    followed by the two separate half-sweeps, on every multigrid level, for
-    odd and even z extents (both row parities at the z faces)."""
+@pytest.mark.parametrize("shape,seed", [((41, 37, 45), 1), ((33, 20, 18), 2),
+                                        ((20, 19, 2), 4)])
+def test_fused_kernels_are_bit_identical(shape, seed):
+    """Each fused kernel of the mixed path writes the bits of the separate
+    launches it replaces, on every multigrid level, for odd and even z
+    extents (both row parities at the z faces) and a grid whose coarse
+    levels reach size-1 axes (the per-node prolongation takes over there):
+    the first Gauss-Seidel pair from a zero correction, the float4 colour-0
+    residual, the windowed prolongation, and the direction update fused into
+    the operator apply (direction, L p and the inner-product partials)."""
     import ctypes
     from ion_gym_gb300 import _lib
     from ion_gym_gb300.physics.mixed import MixedSession
@@ -89,8 +93,7 @@ def test_fused_zero_start_pair_is_bit_identical(shape, seed):
     rings = [masks[i] for i in sorted(masks)]
     with MixedSession(metal, len(rings)) as s:
         s.solve_bases(rings, V, ACC)
-        bad = ctypes.c_longlong(-1)
-        st = _lib.lib().ig_mixed_check_zero_pair(s._h, len(rings),
-                                                 ctypes.byref(bad))
-        _lib.check(st, "ig_mixed_check_zero_pair")
-    assert bad.value == 0
+        bad = (ctypes.c_longlong * 4)(-1, -1, -1, -1)
+        st = _lib.lib().ig_mixed_check_fused(s._h, len(rings), bad)
+        _lib.check(st, "ig_mixed_check_fused")
+    assert list(bad) == [0, 0, 0, 0]
