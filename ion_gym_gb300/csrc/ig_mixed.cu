@@ -613,27 +613,32 @@ k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
   const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
   const float* eb = ec + blockIdx.y * cstride;
   const LerpF x = pa(i, C.nx), y = pa(j, C.ny);
-  int xi[2], yi[2];
-  float xw[2], yw[2];
-  int nxw = 0, nyw = 0;
-  if (x.t != 1.f) { xi[nxw] = x.a0; xw[nxw++] = 1.f - x.t; }
-  if (x.t != 0.f) { xi[nxw] = x.a1; xw[nxw++] = x.t; }
-  if (y.t != 1.f) { yi[nyw] = y.a0; yw[nyw++] = 1.f - y.t; }
-  if (y.t != 0.f) { yi[nyw] = y.a1; yw[nyw++] = y.t; }
-  // z weights of the four fine nodes as offsets v = kc - m0 into the window
-  int zv[4][2];
-  float zw[4][2];
-  int nzw[4];
+  // the nonzero x (y) weights in order: a0 with 1 - t unless t = 1, then a1
+  // with t unless t = 0 (t is 0, 1/2 or 1)
+  const int xi[2] = {x.t == 1.f ? x.a1 : x.a0, x.a1};
+  const float xw[2] = {x.t == 1.f ? x.t : 1.f - x.t, x.t};
+  const int nxw = (x.t != 0.f && x.t != 1.f) ? 2 : 1;
+  const int yi[2] = {y.t == 1.f ? y.a1 : y.a0, y.a1};
+  const float yw[2] = {y.t == 1.f ? y.t : 1.f - y.t, y.t};
+  const int nyw = (y.t != 0.f && y.t != 1.f) ? 2 : 1;
+  // z weights of the four fine nodes: fine node u reads window slots u
+  // (weight wl) and u + 1 (weight wh, skipped when 0).  pa() gives
+  // a0 = m0 + u with weights 1 - t, t (t = 0 or 1/2), or at the top face
+  // a1 = m0 + u alone with weight 1.
+  float wl[4], wh[4];
 #pragma unroll
   for (int u = 0; u < 4; u++) {
     const LerpF z = pa(2 * (m0 + u) + pc, C.nz);
-    nzw[u] = 0;
-    if (z.t != 1.f) { zv[u][nzw[u]] = z.a0 - m0; zw[u][nzw[u]++] = 1.f - z.t; }
-    if (z.t != 0.f) { zv[u][nzw[u]] = z.a1 - m0; zw[u][nzw[u]++] = z.t; }
+    const bool top = z.t == 1.f;
+    wl[u] = top ? z.t : 1.f - z.t;
+    wh[u] = top ? 0.f : z.t;
   }
   float acc[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int a = 0; a < nxw; a++)
-    for (int b = 0; b < nyw; b++) {
+#pragma unroll
+  for (int a = 0; a < 2; a++)
+#pragma unroll
+    for (int b = 0; b < 2; b++) {
+      if (a >= nxw || b >= nyw) continue;
       const uint32_t row = ((uint32_t)xi[a] * C.ny + yi[b]) * C.H + (m0 >> 1);
       const int ca = (xi[a] + yi[b] + m0) & 1;
       const float* A = eb + (size_t)ca * C.csz + row;
@@ -648,7 +653,8 @@ k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
 #pragma unroll
       for (int u = 0; u < 4; u++) {
         float zs = 0.f;
-        for (int q = 0; q < nzw[u]; q++) zs += zw[u][q] * cv[zv[u][q]];
+        zs += wl[u] * cv[u];
+        if (wh[u] != 0.f) zs += wh[u] * cv[u + 1];
         acc[u] += w * zs;
       }
     }
@@ -723,12 +729,61 @@ __global__ void k_split_mask(const uint8_t* __restrict__ nat, SGeo G, uint8_t* _
 
 // ---- FP64 refinement kernels (natural phi64, split g32 / e32) -----------
 
+// sum(neighbours) - 6 * centre of seven FP64 values v[0..5], v[6], times
+// (float) nscale, evaluated exactly in 64-bit fixed point and rounded once
+// to float: every value is M * 2^(e - 1075) (53-bit significand M), so with
+// emax the largest of the seven biased exponents each value is
+// (M << 6) >> (emax - e) units of 2^(emax - 1081), exact except for bits
+// below that unit (at most 7 * 2^-59 of the largest value in all -- the
+// seven FP64 additions and products of the plain expression round at about
+// 2^-53 of it each).  |M << 6| < 2^59, so the sum of six and six times the
+// centre stay below 2^62 and their difference fits int64.  GB300 issues
+// FP64 at about 1/64 of its integer rate; this takes the seven FP64
+// operations of the expression off the FP64 pipe.  Returns false (use the
+// FP64 expression) for non-finite values and for largest magnitudes outside
+// [2^-68, 2^121], where the float scaling would leave the normal range.
+__device__ __forceinline__ bool resid_fixed(const double v[7], float nscale, float& out) {
+  unsigned long long b[7];
+  int e[7];
+  int emax = 0;
+#pragma unroll
+  for (int q = 0; q < 7; q++) {
+    b[q] = static_cast<unsigned long long>(__double_as_longlong(v[q]));
+    e[q] = static_cast<int>(static_cast<unsigned>(b[q] >> 52) & 0x7ffu);
+    emax = max(emax, e[q]);
+  }
+  if (emax == 0) {  // zeros and subnormals only
+    out = 0.f;
+    return true;
+  }
+  if (emax < 955 || emax > 1144) return false;
+  long long f[7];
+#pragma unroll
+  for (int q = 0; q < 7; q++) {
+    const unsigned long long m =
+        e[q] ? ((b[q] & 0x000fffffffffffffULL) | 0x0010000000000000ULL) << 6 : 0ULL;
+    const int d = emax - e[q];
+    const long long a = d < 64 ? static_cast<long long>(m >> d) : 0LL;
+    f[q] = static_cast<long long>(b[q]) < 0 ? -a : a;
+  }
+  const long long r = (((f[0] + f[1]) + (f[2] + f[3])) + (f[4] + f[5])) - ((f[6] << 2) + (f[6] << 1));
+  if (r == 0) {
+    out = 0.f;
+    return true;
+  }
+  // r * 2^(emax - 1081), exponent field emax - 954 in 1..190
+  out = __ll2float_rn(r) * __int_as_float((emax - 954) << 23) * nscale;
+  return true;
+}
+
 // g32 = -(float) (scale * r64(phi)) at free nodes, 0 at metal; r64 is the
 // reference's fine residual with theta None (kind kPlain: sum - 6 phi; the
-// Shortley-Weller form is half of it and is scaled by 2 through `scale`).
+// Shortley-Weller form is half of it and is scaled by 2 through `scale`,
+// nscale = -(float) scale, a power of two).  The residual is formed exactly
+// (resid_fixed) and rounded once to float.
 __global__ void __launch_bounds__(kT)
 k_resid64(const double* __restrict__ phi, const uint8_t* __restrict__ fixed,
-          SGeo G, float* __restrict__ g, double scale, size_t nstride,
+          SGeo G, float* __restrict__ g, double scale, float nscale, size_t nstride,
           size_t pstride) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= G.n) return;
@@ -739,23 +794,29 @@ k_resid64(const double* __restrict__ phi, const uint8_t* __restrict__ fixed,
   float out = 0.f;
   if (!fixed[t]) {
     const double* p = phi + blockIdx.y * nstride;
-    const size_t sx = (size_t)G.ny * G.nz, sy = G.nz;
-    const size_t row = (size_t)i * sx + (size_t)j * sy;
-    const double s = ((p[(size_t)lo_i(i, G.nx) * sx + (size_t)j * sy + k] +
-                       p[(size_t)hi_i(i, G.nx) * sx + (size_t)j * sy + k]) +
-                      (p[(size_t)i * sx + (size_t)lo_i(j, G.ny) * sy + k] +
-                       p[(size_t)i * sx + (size_t)hi_i(j, G.ny) * sy + k])) +
-                     (p[row + lo_i(k, G.nz)] + p[row + hi_i(k, G.nz)]);
-    const double r = s - 6.0 * p[t];
-    out = (float)(-scale * r);
+    const uint32_t sx = (uint32_t)G.ny * G.nz, sy = G.nz;
+    const uint32_t row = (uint32_t)i * sx + (uint32_t)j * sy;
+    double v[7];
+    v[0] = p[(uint32_t)lo_i(i, G.nx) * sx + (uint32_t)j * sy + k];
+    v[1] = p[(uint32_t)hi_i(i, G.nx) * sx + (uint32_t)j * sy + k];
+    v[2] = p[(uint32_t)i * sx + (uint32_t)lo_i(j, G.ny) * sy + k];
+    v[3] = p[(uint32_t)i * sx + (uint32_t)hi_i(j, G.ny) * sy + k];
+    v[4] = p[row + lo_i(k, G.nz)];
+    v[5] = p[row + hi_i(k, G.nz)];
+    v[6] = p[t];
+    if (!resid_fixed(v, nscale, out)) {
+      const double s = ((v[0] + v[1]) + (v[2] + v[3])) + (v[4] + v[5]);
+      out = (float)(-scale * (s - 6.0 * v[6]));
+    }
   }
   g[blockIdx.y * pstride + (size_t)scol(i, j, k) * G.csz + sidx(G, i, j, k)] = out;
 }
 
-// phi64 += e32 at free nodes; the applied change |phi_new - phi_old| is
-// measured in FP64 and its per-problem maximum goes to dmax[b] (the
-// refinement's convergence norm, the analogue of the V-cycle's full-cycle
-// change, multigrid3d.py:702).
+// phi64 += e32 at free nodes; the per-problem maximum of |e32| (exact in
+// FP64; the applied change |phi_new - phi_old| differs from it by at most
+// half an ulp of phi) goes to dmax[b] (the refinement's convergence norm,
+// the analogue of the V-cycle's full-cycle change, multigrid3d.py:702).
+// One FP64 operation per node.
 __global__ void __launch_bounds__(kT)
 k_update64(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
            const float* __restrict__ e, SGeo G, unsigned long long* dmax,
@@ -768,12 +829,26 @@ k_update64(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
     const int i = (int)fdivu(ij, G.dny);
     const int j = (int)(ij - (uint32_t)i * G.dny.d);
     const float d = e[blockIdx.y * pstride + (size_t)scol(i, j, k) * G.csz + sidx(G, i, j, k)];
+    // (double) d by its bits for zeros and normal floats (exponent rebias,
+    // significand moved up 29 bits); subnormals, infinities and NaN convert
+    // on the FP64 pipe
+    const unsigned fb = __float_as_uint(d);
+    const unsigned ef = (fb >> 23) & 0xffu;
+    double dd;
+    if (ef - 1u < 254u || (fb & 0x7fffffffu) == 0u) {
+      const unsigned long long sg = static_cast<unsigned long long>(fb & 0x80000000u) << 32;
+      dd = __longlong_as_double(static_cast<long long>(
+          (fb & 0x7fffffffu) == 0u
+              ? sg
+              : sg | (static_cast<unsigned long long>(ef + 896u) << 52) |
+                    (static_cast<unsigned long long>(fb & 0x7fffffu) << 29)));
+    } else {
+      dd = (double)d;
+    }
     double* q = phi + blockIdx.y * nstride + t;
-    const double old = *q;
-    const double nw = old + (double)d;
-    *q = nw;
-    const double ch = nw - old;
-    key = static_cast<unsigned long long>(__double_as_longlong(ch)) & 0x7fffffffffffffffULL;
+    *q = *q + dd;
+    // the norm of the step is max |correction| (the FP64 value added)
+    key = static_cast<unsigned long long>(__double_as_longlong(dd)) & 0x7fffffffffffffffULL;
     if (key > 0x7ff0000000000000ULL) key = 0x7ff0000000000000ULL;  // NaN: never converged
   }
   key = warp_max_u64(key);
@@ -909,7 +984,7 @@ k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
 // read once and p is written once.  p_old and pn are different arrays (a
 // thread of one colour reads the other colour's p_old while that colour's
 // threads store theirs).  Same expressions as the two kernels, same bits.
-__global__ void __launch_bounds__(kT)
+__global__ void __launch_bounds__(kT, 4)
 k_cg_matvec_dir(const float* __restrict__ z, const float* __restrict__ po,
                 float* __restrict__ pn, const double* __restrict__ scal,
                 const float* __restrict__ g, const uint8_t* __restrict__ mask, SGeo G,
@@ -1368,7 +1443,7 @@ struct Session {
     MLevel& f = lv[0];
     const size_t nstride = f.G.n;
     const dim3 gn(nblk(f.G.n), B);
-    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, nstride, f.pstride);
+    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, nstride, f.pstride);
     for (int v = 0; v < vcycles; v++) vcycle(0, v == 0);
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
     k_update64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.e.p, f.G, dmax.p, nstride, f.pstride);
@@ -1378,7 +1453,7 @@ struct Session {
   void cg_init() {
     MLevel& f = lv[0];
     const dim3 gn(nblk(f.G.n), B);
-    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, f.G.n, f.pstride);
+    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, f.G.n, f.pstride);
     MK(cudaMemsetAsync(xb.p, 0, f.pstride * B * 4, s));
     MK(cudaMemsetAsync(pb.p, 0, f.pstride * B * 4, s));
     MK(cudaMemsetAsync(qb.p, 0, f.pstride * B * 4, s));
@@ -1419,7 +1494,7 @@ struct Session {
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
     k_update64<<<gn, kT, 0, s>>>(phi.p, fixed.p, xb.p, f.G, dmax.p, f.G.n, f.pstride);
     MK(cudaMemsetAsync(xb.p, 0, f.pstride * B * 4, s));
-    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, f.G.n, f.pstride);
+    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, f.G.n, f.pstride);
   }
 
   void step() {
