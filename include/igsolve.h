@@ -198,12 +198,13 @@ int ig_mixed_time_gs(void *handle, int n_problems, int pairs,
  * [1] = the float4 colour-0 residual vs the per-slot one, [2] = the
  * windowed prolongation vs the per-node gather, [3] = the direction update
  * fused into the operator apply vs the two kernels (direction, L p and the
- * block partials of the inner products) -- each the number of 32-bit words
+ * block partials of the inner products), [4] = the four-node restriction
+ * of the colour-0 residual vs the per-node one -- each the number of 32-bit words
  * that differ over every multigrid level, 0 when bit-identical.
  * Flexible-CG sessions only; no reference counterpart (a self-check of this
  * library's kernel fusion). */
 int ig_mixed_check_fused(void *handle, int n_problems,
-                         long long mismatches[4]);
+                         long long mismatches[5]);
 
 /* ig_cascadic_relres for callers that cannot allocate device memory (no
  * counterpart in the reference).  Some callers may not call cudaMalloc, or

@@ -445,6 +445,105 @@ k_restrict0(const float* __restrict__ r0, SGeo F, float* __restrict__ gc, SGeo C
   gc[blockIdx.y * cstride + (size_t)c * C.csz + sidx(C, ic, jc, kc)] = 0.5f * acc;
 }
 
+// The 13-tap sum of one coarse node (k_restrict0's loop).
+__device__ __forceinline__ float restrict0_node(const float* __restrict__ rb, const SGeo& F,
+                                                int ic, int jc, int kc) {
+  float acc = 0.f;
+#pragma unroll
+  for (int di = -1; di <= 1; di++) {
+    const int ii = min(max(2 * ic + di, 0), F.nx - 1);
+    const float wi = di == 0 ? 1.f : 0.5f;
+#pragma unroll
+    for (int dj = -1; dj <= 1; dj++) {
+      const int jj = min(max(2 * jc + dj, 0), F.ny - 1);
+      const float wj = dj == 0 ? 1.f : 0.5f;
+#pragma unroll
+      for (int dk = -1; dk <= 1; dk++) {
+        const int kk = min(max(2 * kc + dk, 0), F.nz - 1);
+        if ((ii + jj + kk) & 1) continue;
+        const float wk = dk == 0 ? 1.f : 0.5f;
+        acc += wi * wj * wk * rb[sidx(F, ii, jj, kk)];
+      }
+    }
+  }
+  return acc;
+}
+
+// k_restrict0 for four consecutive coarse z nodes kc = 4g .. 4g+3 of one
+// coarse row per thread.  Away from the faces (no clamped tap) the 13 taps
+// of the four nodes are nine 16-byte row loads and four edge slots: around
+// fine centre (2ic, 2jc, 2kc) the colour-0 taps are slot kc of rows (0, 0)
+// and (+-1, +-1), and slots kc - 1 and kc of rows (+-1, 0) and (0, +-1)
+// (their colour-0 nodes have odd k).  Taps are summed in k_restrict0's
+// (di, dj, dk) order with its weights, so the bits are the same; groups
+// that touch a face use that loop per node.  The four results go to the
+// coarse split layout as two 8-byte stores (kc alternates colour).
+__global__ void __launch_bounds__(kT)
+k_restrict0_4(const float* __restrict__ r0, SGeo F, float* __restrict__ gc, SGeo C,
+              size_t cstride) {
+  const uint32_t G4 = (uint32_t)(C.nz + 3) >> 2;
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= (uint32_t)C.nx * C.ny * G4) return;
+  const uint32_t ij = t / G4;
+  const int kc0 = 4 * (int)(t - ij * G4);
+  const int ic = (int)fdivu(ij, C.dny);
+  const int jc = (int)(ij - (uint32_t)ic * C.dny.d);
+  const float* rb = r0 + blockIdx.y * (size_t)F.csz;
+  float* gb = gc + blockIdx.y * cstride;
+  const bool inner = ic >= 1 && 2 * ic + 1 <= F.nx - 1 && jc >= 1 && 2 * jc + 1 <= F.ny - 1 &&
+                     kc0 >= 1 && 2 * (kc0 + 3) + 1 <= F.nz - 1;
+  if (!inner) {
+    for (int u = 0; u < 4; u++) {
+      const int kc = kc0 + u;
+      if (kc >= C.nz) break;
+      gb[(size_t)scol(ic, jc, kc) * C.csz + sidx(C, ic, jc, kc)] =
+          0.5f * restrict0_node(rb, F, ic, jc, kc);
+    }
+    return;
+  }
+  auto row = [&](int di, int dj) {
+    return rb + ((uint32_t)(2 * ic + di) * F.ny + (uint32_t)(2 * jc + dj)) * F.H + kc0;
+  };
+  float a[4] = {0.f, 0.f, 0.f, 0.f};
+  // one tap per node from slot kc of a row, weight w
+  auto at = [&](const float* r, float w) {
+    const float4 v = ld4(r);
+    a[0] += w * v.x;
+    a[1] += w * v.y;
+    a[2] += w * v.z;
+    a[3] += w * v.w;
+  };
+  // two taps per node from slots kc - 1 and kc of a row (dk = -1, +1)
+  auto at2 = [&](const float* r, float w) {
+    const float4 v = ld4(r);
+    const float m = r[-1];
+    a[0] += w * m;
+    a[0] += w * v.x;
+    a[1] += w * v.x;
+    a[1] += w * v.y;
+    a[2] += w * v.y;
+    a[2] += w * v.z;
+    a[3] += w * v.z;
+    a[3] += w * v.w;
+  };
+  at(row(-1, -1), 0.25f);
+  at2(row(-1, 0), 0.25f);
+  at(row(-1, 1), 0.25f);
+  at2(row(0, -1), 0.25f);
+  at(row(0, 0), 1.f);
+  at2(row(0, 1), 0.25f);
+  at(row(1, -1), 0.25f);
+  at2(row(1, 0), 0.25f);
+  at(row(1, 1), 0.25f);
+  // kc0 is even: nodes kc0, kc0 + 2 share a colour (slots kc0/2, kc0/2 + 1),
+  // kc0 + 1, kc0 + 3 the other
+  const int ca = scol(ic, jc, kc0);
+  const uint32_t cs = ((uint32_t)ic * C.ny + jc) * C.H + (kc0 >> 1);
+  *reinterpret_cast<float2*>(gb + (size_t)ca * C.csz + cs) = make_float2(0.5f * a[0], 0.5f * a[2]);
+  *reinterpret_cast<float2*>(gb + (size_t)(1 - ca) * C.csz + cs) =
+      make_float2(0.5f * a[1], 0.5f * a[3]);
+}
+
 // r = g - A e on natural layout (0 at metal).
 __global__ void __launch_bounds__(kT)
 k_resid(const float* __restrict__ e, const float* __restrict__ g,
@@ -1084,17 +1183,21 @@ k_cg_reduce(const double* __restrict__ part, int nparts, int stride,
   }
 }
 
-// x += alpha p; g += alpha q
+// x += alpha p; g += alpha q (float4)
 __global__ void __launch_bounds__(kT)
 k_cg_update(float* __restrict__ x, float* __restrict__ g, const float* __restrict__ p,
             const float* __restrict__ q, const double* __restrict__ scal,
             size_t pstride, uint32_t n) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
-  if (t >= n) return;
+  if (t >= n / 4) return;  // n: a multiple of 4 (split rows are)
   const float al = (float)scal[4 * blockIdx.y + 1];
-  const size_t o = blockIdx.y * pstride + t;
-  x[o] += al * p[o];
-  g[o] += al * q[o];
+  const size_t o = blockIdx.y * pstride + 4 * (size_t)t;
+  float4 xv = ld4(x + o), gv = ld4(g + o);
+  const float4 pv = ld4(p + o), qv = ld4(q + o);
+  xv.x += al * pv.x; xv.y += al * pv.y; xv.z += al * pv.z; xv.w += al * pv.w;
+  gv.x += al * qv.x; gv.y += al * qv.y; gv.z += al * qv.z; gv.w += al * qv.w;
+  *reinterpret_cast<float4*>(x + o) = xv;
+  *reinterpret_cast<float4*>(g + o) = gv;
 }
 
 // ---- host side ----------------------------------------------------------
@@ -1419,7 +1522,8 @@ struct Session {
       else
         k_resid0_4<<<dim3(nblk(a.G.csz / 4), B), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G,
                                                             a.r.p, a.pstride);
-      k_restrict0<<<dim3(nblk(b.G.n), B), kT, 0, s>>>(a.r.p, a.G, b.g.p, b.G, b.pstride);
+      k_restrict0_4<<<dim3(nblk((uint32_t)b.G.nx * b.G.ny * ((b.G.nz + 3) / 4)), B), kT, 0, s>>>(
+          a.r.p, a.G, b.g.p, b.G, b.pstride);
     } else {
       k_resid<<<gn, kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p, a.pstride, a.rstride);
       k_restrict<<<dim3(nblk(b.G.n), B), kT, 0, s>>>(a.r.p, a.G, b.g.p, b.G, a.rstride, b.pstride);
@@ -1485,7 +1589,8 @@ struct Session {
                                                   f.pstride);
       }
       k_cg_reduce<<<B, kT, 0, s>>>(part.p, 2 * (int)nb4, 2, scal.p, 0);
-      k_cg_update<<<gv, kT, 0, s>>>(xb.p, f.g.p, pcur, qb.p, scal.p, f.pstride, n);
+      k_cg_update<<<dim3(nblk(n / 4), B), kT, 0, s>>>(xb.p, f.g.p, pcur, qb.p, scal.p, f.pstride,
+                                                     n);
     }
     // the next step (a replay of this graph) starts from pb
     if (pcur != pb.p)
@@ -1695,7 +1800,7 @@ int ig_mixed_time_gs(void* handle, int n_problems, int pairs, double* ms_per_lau
   }
 }
 
-int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[4]) {
+int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[5]) {
   set_last_error("");
   Session* S = static_cast<Session*>(handle);
   if (!S || !mismatches || n_problems < 1 || n_problems > S->bmax || S->method != 1 ||
@@ -1708,8 +1813,8 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[4]) 
     const int B = n_problems;
     cudaStream_t s = S->s;
     Buf<unsigned long long> bad;
-    bad.alloc(4, s);
-    MK(cudaMemsetAsync(bad.p, 0, 32, s));
+    bad.alloc(5, s);
+    MK(cudaMemsetAsync(bad.p, 0, 40, s));
     long launches = 0;
     auto diff = [&](const void* a, const void* b, size_t words, int slot) {
       k_count_diff<<<dim3((unsigned)((words + kT - 1) / kT), 1), kT, 0, s>>>(
@@ -1740,6 +1845,13 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[4]) 
       k_resid0_4<<<dim3(nblk(a.G.csz / 4), B), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, a.r.p,
                                                           a.pstride);
       diff(a.r.p, scrA, (size_t)a.G.csz * B, 1);
+      launches += 2;
+      // the restriction of that residual to the coarse right-hand side
+      k_restrict0<<<dim3(nblk(b.G.n), B), kT, 0, s>>>(a.r.p, a.G, b.g.p, b.G, b.pstride);
+      MK(cudaMemcpyAsync(scrA, b.g.p, b.pstride * B * 4, cudaMemcpyDeviceToDevice, s));
+      k_restrict0_4<<<dim3(nblk((uint32_t)b.G.nx * b.G.ny * ((b.G.nz + 3) / 4)), B), kT, 0, s>>>(
+          a.r.p, a.G, b.g.p, b.G, b.pstride);
+      diff(b.g.p, scrA, b.pstride * B, 4);
       launches += 2;
       // the fused first pair from a zero correction (a stand-in correction
       // left over from an earlier cycle: both ways must overwrite all of it)
@@ -1773,11 +1885,11 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[4]) 
       diff(S->part.p, part2.p, 2 * nparts, 3);
       launches += 3;
     }
-    unsigned long long h[4] = {0, 0, 0, 0};
-    MK(cudaMemcpyAsync(h, bad.p, 32, cudaMemcpyDeviceToHost, s));
+    unsigned long long h[5] = {0, 0, 0, 0, 0};
+    MK(cudaMemcpyAsync(h, bad.p, 40, cudaMemcpyDeviceToHost, s));
     MK(cudaStreamSynchronize(s));
     g_mixed_launches.fetch_add(launches);
-    for (int q = 0; q < 4; q++) mismatches[q] = (long long)h[q];
+    for (int q = 0; q < 5; q++) mismatches[q] = (long long)h[q];
     return (int)IG_OK;
   } catch (int code) {
     return code;

@@ -81,8 +81,9 @@ def test_fused_kernels_are_bit_identical(shape, seed):
     extents (both row parities at the z faces) and a grid whose coarse
     levels reach size-1 axes (the per-node prolongation takes over there):
     the first Gauss-Seidel pair from a zero correction, the float4 colour-0
-    residual, the windowed prolongation, and the direction update fused into
-    the operator apply (direction, L p and the inner-product partials)."""
+    residual, the windowed prolongation, the direction update fused into
+    the operator apply (direction, L p and the inner-product partials), and
+    the four-node restriction of the colour-0 residual."""
     import ctypes
     from ion_gym_gb300 import _lib
     from ion_gym_gb300.physics.mixed import MixedSession
@@ -93,7 +94,7 @@ def test_fused_kernels_are_bit_identical(shape, seed):
     rings = [masks[i] for i in sorted(masks)]
     with MixedSession(metal, len(rings)) as s:
         s.solve_bases(rings, V, ACC)
-        bad = (ctypes.c_longlong * 4)(-1, -1, -1, -1)
+        bad = (ctypes.c_longlong * 5)(-1, -1, -1, -1, -1)
         st = _lib.lib().ig_mixed_check_fused(s._h, len(rings), bad)
         _lib.check(st, "ig_mixed_check_fused")
-    assert list(bad) == [0, 0, 0, 0]
+    assert list(bad) == [0, 0, 0, 0, 0]
