@@ -950,15 +950,7 @@ k_update64(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
     key = static_cast<unsigned long long>(__double_as_longlong(dd)) & 0x7fffffffffffffffULL;
     if (key > 0x7ff0000000000000ULL) key = 0x7ff0000000000000ULL;  // NaN: never converged
   }
-  key = warp_max_u64(key);
-  __shared__ unsigned long long red[kT / 32];
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = key;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    key = threadIdx.x < kT / 32 ? red[threadIdx.x] : 0ull;
-    key = warp_max_u64(key);
-    if (threadIdx.x == 0 && key) atomicMax(dmax + blockIdx.y, key);
-  }
+  block_max_to(key, dmax + blockIdx.y);
 }
 
 // phi64[b] = Dirichlet values of problem b at metal, 0 elsewhere; for a
