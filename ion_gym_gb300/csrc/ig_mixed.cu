@@ -911,44 +911,61 @@ k_resid64(const double* __restrict__ phi, const uint8_t* __restrict__ fixed,
   g[blockIdx.y * pstride + (size_t)scol(i, j, k) * G.csz + sidx(G, i, j, k)] = out;
 }
 
+
+// float -> double by its bits for zeros and normal floats (exponent rebias,
+// significand moved up 29 bits); subnormals, infinities and NaN convert on
+// the FP64 pipe.
+__device__ __forceinline__ double widen(float d) {
+  const unsigned fb = __float_as_uint(d);
+  const unsigned ef = (fb >> 23) & 0xffu;
+  if ((fb & 0x7fffffffu) == 0u)
+    return __longlong_as_double(static_cast<long long>(static_cast<unsigned long long>(fb) << 32));
+  if (ef - 1u < 254u)
+    return __longlong_as_double(static_cast<long long>(
+        (static_cast<unsigned long long>(fb & 0x80000000u) << 32) |
+        (static_cast<unsigned long long>(ef + 896u) << 52) |
+        (static_cast<unsigned long long>(fb & 0x7fffffu) << 29)));
+  return (double)d;
+}
+
 // phi64 += e32 at free nodes; the per-problem maximum of |e32| (exact in
 // FP64; the applied change |phi_new - phi_old| differs from it by at most
 // half an ulp of phi) goes to dmax[b] (the refinement's convergence norm,
 // the analogue of the V-cycle's full-cycle change, multigrid3d.py:702).
-// One FP64 operation per node.
+// One FP64 operation per node.  Eight consecutive natural nodes
+// k0 = 8g .. 8g+7 of one row per thread: their corrections are float4 group
+// g of each colour's split row (k0 is even, so colour (i + j) & 1 holds k0,
+// k0+2, .. and the other colour k0+1, k0+3, ..), the potentials and masks
+// 64 and 8 contiguous bytes.  One block maximum per 2048 nodes.
 __global__ void __launch_bounds__(kT)
-k_update64(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
-           const float* __restrict__ e, SGeo G, unsigned long long* dmax,
-           size_t nstride, size_t pstride) {
+k_update64_8(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
+             const float* __restrict__ e, SGeo G, unsigned long long* dmax,
+             size_t nstride, size_t pstride) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   unsigned long long key = 0;
-  if (t < G.n && !fixed[t]) {
-    const uint32_t ij = fdivu(t, G.dnz);
-    const int k = (int)(t - ij * G.dnz.d);
-    const int i = (int)fdivu(ij, G.dny);
-    const int j = (int)(ij - (uint32_t)i * G.dny.d);
-    const float d = e[blockIdx.y * pstride + (size_t)scol(i, j, k) * G.csz + sidx(G, i, j, k)];
-    // (double) d by its bits for zeros and normal floats (exponent rebias,
-    // significand moved up 29 bits); subnormals, infinities and NaN convert
-    // on the FP64 pipe
-    const unsigned fb = __float_as_uint(d);
-    const unsigned ef = (fb >> 23) & 0xffu;
-    double dd;
-    if (ef - 1u < 254u || (fb & 0x7fffffffu) == 0u) {
-      const unsigned long long sg = static_cast<unsigned long long>(fb & 0x80000000u) << 32;
-      dd = __longlong_as_double(static_cast<long long>(
-          (fb & 0x7fffffffu) == 0u
-              ? sg
-              : sg | (static_cast<unsigned long long>(ef + 896u) << 52) |
-                    (static_cast<unsigned long long>(fb & 0x7fffffu) << 29)));
-    } else {
-      dd = (double)d;
+  if (t < (G.csz >> 2)) {
+    const uint32_t ij = fdivu(t, G.dH4);
+    const int k0 = 8 * (int)(t - ij * G.dH4.d);
+    if (k0 < G.nz) {
+      const int i = (int)fdivu(ij, G.dny);
+      const int j = (int)(ij - (uint32_t)i * G.dny.d);
+      const int p0 = (i + j) & 1;
+      const float* eb = e + blockIdx.y * pstride + ij * (uint32_t)G.H + (k0 >> 1);
+      const float4 ea = ld4(eb + (size_t)p0 * G.csz), eo = ld4(eb + (size_t)(1 - p0) * G.csz);
+      const float ev[8] = {ea.x, eo.x, ea.y, eo.y, ea.z, eo.z, ea.w, eo.w};
+      const uint32_t nat = ij * (uint32_t)G.nz + k0;
+      double* q = phi + blockIdx.y * nstride + nat;
+#pragma unroll
+      for (int u = 0; u < 8; u++) {
+        if (k0 + u >= G.nz || fixed[nat + u]) continue;
+        const double dd = widen(ev[u]);
+        q[u] = q[u] + dd;
+        unsigned long long kk =
+            static_cast<unsigned long long>(__double_as_longlong(dd)) & 0x7fffffffffffffffULL;
+        if (kk > 0x7ff0000000000000ULL) kk = 0x7ff0000000000000ULL;  // NaN: never converged
+        key = max(key, kk);
+      }
     }
-    double* q = phi + blockIdx.y * nstride + t;
-    *q = *q + dd;
-    // the norm of the step is max |correction| (the FP64 value added)
-    key = static_cast<unsigned long long>(__double_as_longlong(dd)) & 0x7fffffffffffffffULL;
-    if (key > 0x7ff0000000000000ULL) key = 0x7ff0000000000000ULL;  // NaN: never converged
   }
   block_max_to(key, dmax + blockIdx.y);
 }
@@ -1542,7 +1559,8 @@ struct Session {
     k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, nstride, f.pstride);
     for (int v = 0; v < vcycles; v++) vcycle(0, v == 0);
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
-    k_update64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.e.p, f.G, dmax.p, nstride, f.pstride);
+    k_update64_8<<<dim3(nblk(f.G.csz / 4), B), kT, 0, s>>>(phi.p, fixed.p, f.e.p, f.G, dmax.p,
+                                                         nstride, f.pstride);
   }
 
   // the flexible CG: once per solve, the FP64 residual and zero state
@@ -1589,7 +1607,8 @@ struct Session {
       MK(cudaMemcpyAsync(pb.p, pcur, f.pstride * B * 4, cudaMemcpyDeviceToDevice, s));
     const dim3 gn(nblk(f.G.n), B);
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
-    k_update64<<<gn, kT, 0, s>>>(phi.p, fixed.p, xb.p, f.G, dmax.p, f.G.n, f.pstride);
+    k_update64_8<<<dim3(nblk(f.G.csz / 4), B), kT, 0, s>>>(phi.p, fixed.p, xb.p, f.G, dmax.p,
+                                                         f.G.n, f.pstride);
     MK(cudaMemsetAsync(xb.p, 0, f.pstride * B * 4, s));
     k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, f.G.n, f.pstride);
   }
