@@ -475,22 +475,38 @@ def run_uneven(a):
     {33,65,97,129,193,257}, 2-16 random electrodes at U(-100,100) V, each
     solved to 1e-9 of its span by the mixed path; the geometries run
     concurrently (one resident session and CUDA stream each, `workers`
-    at a time)."""
+    at a time).  Each deck arrives as host buffers (metal mask, Dirichlet
+    values) in pinned memory, as a serving caller hands them over, and its
+    potential is returned into a pinned host buffer: every upload, session
+    build and download is inside the timed region."""
     import concurrent.futures as cf
     import torch
+    from ion_gym_gb300 import _lib
     from ion_gym_gb300.workloads import random_deck
     from ion_gym_gb300.physics.mixed import MixedSession
     torch.cuda.set_device(0)
+    L = _lib.lib()
     rng = np.random.default_rng(2026)
     sides = rng.choice([33, 65, 97, 129, 193, 257], 64)
     nel = rng.integers(2, 17, 64)
-    decks = [random_deck(1000 + i, int(s), int(k))
-             for i, (s, k) in enumerate(zip(sides, nel))]
+
+    def pinned(x):
+        t = torch.empty(x.shape, dtype=getattr(torch, str(x.dtype))).pin_memory()
+        h = t.numpy()
+        h[...] = x
+        return h
+
+    decks = []
+    for q, (sd, k) in enumerate(zip(sides, nel)):
+        fixed, val = random_deck(1000 + q, int(sd), int(k))
+        span = max(float(val.max() - val.min()), 1.0)
+        decks.append((pinned(fixed), pinned(val), pinned(np.zeros(val.shape)), span))
 
     def solve(d):
-        fixed, val = d
+        fixed, val, out, span = d
         with MixedSession(fixed, 1) as s:
-            return s.solve_values(val, 1e-9)
+            s.solve_values(val, 1e-9, out=out, span=span)
+            return s.last_steps
 
     # largest geometries first (longest-processing-time order), so the
     # small ones fill the device while the last large ones finish
@@ -499,10 +515,16 @@ def run_uneven(a):
     with cf.ThreadPoolExecutor(workers) as ex:
         list(ex.map(solve, decks[:workers]))              # warm-up
         torch.cuda.synchronize()
+        clocks = Clocks(0)
+        launches0 = L.ig_launch_count() + _mixed_launches(L)
+        clocks.start()
         t0 = time.perf_counter()
-        list(ex.map(solve, [decks[q] for q in order]))
+        steps = list(ex.map(solve, [decks[q] for q in order]))
+        torch.cuda.synchronize()
         el = time.perf_counter() - t0
-    nodes = sum(int(s) ** 3 for s in sides)
+        ck = clocks.stop()
+        launches = L.ig_launch_count() + _mixed_launches(L) - launches0
+    nodes = sum(int(sd) ** 3 for sd in sides)
     print(json.dumps({
         "metric": METRIC, "value": 64 / el, "unit": "solves/s", "n_gpus": 1,
         "steps": 1, "warmup": 1, "ms_per_step": 1e3 * el,
@@ -510,9 +532,16 @@ def run_uneven(a):
         "dtype": "f32 sweeps + f64 refinement",
         "data": "synthetic (64 seeded random decks)",
         "config": {"workload": "uneven_batch_64_mixed", "sides":
-                   [int(s) for s in sides], "nodes": nodes,
+                   [int(sd) for sd in sides], "nodes": nodes,
                    "accuracy_of_span": 1e-9, "concurrent_sessions": workers,
-                   "order": "largest grid first"}}),
+                   "order": "largest grid first",
+                   "host_buffers": "pinned (mask, values in; potential out)",
+                   "l2": "inputs larger than L2 (the batch holds GBs)"},
+        "refinement_steps": {"min": int(min(steps)), "max": int(max(steps))},
+        "e2e": {"value": 64 / el, "unit": "solves/s",
+                "h2d_bytes_per_step": 9 * nodes, "d2h_bytes_per_step": 8 * nodes},
+        "gpu_launches": int(launches),
+        "clocks": ck}),
         flush=True)
 
 
