@@ -139,12 +139,14 @@ int ig_cascadic_relres(const uint8_t *fixed, const double *val, long nx,
  * problem, multigrid3d.py:233-291, with a different method and stopping
  * rule): n_bases unit bases on the metal union `metal`, basis b at v_basis
  * on masks[b] (n_bases stacked (nx,ny,nz) uint8 masks) and 0 on the rest of
- * the metal.  FP32 red-black multigrid V-cycles (nu1/nu2 Gauss-Seidel pairs,
- * `vcycles` per step) solve for the correction of the FP64 potential, whose
- * FP64 residual is the reference's fine operator with theta None; a basis is
- * done when one step changes its potential by less than `acc` (absolute,
- * volts) anywhere.  Out: phi (n_bases x n float64), refinement steps, and
- * each basis's last change.  IG_NOT_CONVERGED after max_steps. */
+ * the metal.  Flexible conjugate gradients on the FP32 correction,
+ * preconditioned by one FP32 red-black multigrid V-cycle (nu1/nu2
+ * Gauss-Seidel pairs), refine the FP64 potential, whose residual is the
+ * reference's fine operator with theta None (formed exactly); a basis is
+ * done when the last refinement step d and the geometric tail estimate
+ * d * rho / (1 - rho) (rho the observed step ratio) are both below `acc`
+ * (absolute, volts).  Out: phi (n_bases x n float64), refinement steps, and
+ * each basis's last step.  IG_NOT_CONVERGED after max_steps. */
 int ig_mixed_bases(const uint8_t *metal, const uint8_t *masks, int n_bases,
                    double v_basis, long nx, long ny, long nz, int stencil,
                    double acc, int max_steps, int nu1, int nu2, int vcycles,
