@@ -564,7 +564,9 @@ def run_serve(a):
         masks = {k: m for k, m in masks.items() if m.any()}
         masks[max(masks) + 1] = box
         pool.append(masks)
-    srv = FieldServer(workers=a.workers)
+    # the served bases stay in HBM (device results): the consumers -- the
+    # field build, the tracer -- read them there
+    srv = FieldServer(workers=a.workers, results="device")
     for d in pool:                                   # warm: resident sessions
         srv.submit(d).result()
     srv.completed.clear()
@@ -593,7 +595,9 @@ def run_serve(a):
         "dtype": "f32 sweeps + f64 refinement", "data": "synthetic boards",
         "config": {"workload": "serve_poisson_planar_boards",
                    "rate_req_s": a.rate, "duration_s": a.duration,
-                   "workers": a.workers, "shapes": shapes},
+                   "workers": a.workers, "shapes": shapes,
+                   "results": "device (float64 bases stay in HBM)",
+                   "masks": "host numpy, uploaded per request"},
         "latency_ms": {"p50": 1e3 * percentile(total, 50),
                        "p99": 1e3 * percentile(total, 99),
                        "queue_p50": 1e3 * percentile([x[0] for x in lat], 50),

@@ -84,8 +84,11 @@ class MixedSession:
             B = int(masks.shape[0])
             mptr = ptr(masks)
         else:
+            # a list of masks is stacked into the session's pinned staging
+            # buffer (kept for the next call), so the upload runs at the
+            # link's speed
             B = len(masks)
-            stack = np.empty((B,) + self.shape, np.uint8)
+            stack = self._mask_stage(B)
             for b, m in enumerate(masks):
                 stack[b] = np.asarray(m, bool)
             mptr = ptr(stack)
@@ -141,6 +144,14 @@ class MixedSession:
         self._outcome(st, steps.value, dmax, accuracy, span)
         self.last_steps = int(steps.value)
         return phi
+
+    def _mask_stage(self, B):
+        st = getattr(self, "_stage", None)
+        if st is None or st.shape[0] < B:
+            import torch
+            st = torch.empty((B,) + self.shape, dtype=torch.uint8).pin_memory().numpy()
+            self._stage = st
+        return st[:B]
 
     def close(self):
         if self._h:

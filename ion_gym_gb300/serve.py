@@ -61,10 +61,20 @@ class FieldServer:
     of the free memory at start-up).
     session_factory / bytes_fn: the session class and its footprint
     function (MixedSession and session_bytes; replaceable for tests of the
-    admission logic without a GPU)."""
+    admission logic without a GPU).
+    results: "host" -- each basis a float64 numpy array (the reference's
+    solve_bases_mg return); "device" -- each basis a float64 CUDA tensor
+    that stays in HBM for consumers on the GPU (the field build reads bases
+    in place), with no device-to-host copy in the request's latency.
+    Device results are the caller's: they count against free HBM, not
+    against the server's session budget."""
 
     def __init__(self, workers=4, hbm_budget=None, device=0,
-                 session_factory=MixedSession, bytes_fn=session_bytes):
+                 session_factory=MixedSession, bytes_fn=session_bytes,
+                 results="host"):
+        if results not in ("host", "device"):
+            raise ValueError('results must be "host" or "device"')
+        self.results = results
         self.device = device
         self._factory = session_factory
         self._bytes_fn = bytes_fn
@@ -167,8 +177,15 @@ class FieldServer:
                     for m in r.masks.values():
                         metal |= np.asarray(m, bool)
                     sess = self._factory(metal, r.n_bases)
-                phi = sess.solve_bases(list(r.masks.values()), r.v_basis,
-                                       r.accuracy)
+                if self.results == "device":
+                    import torch
+                    out = torch.empty((r.n_bases,) + r.shape, dtype=torch.float64,
+                                      device=f"cuda:{self.device or 0}")
+                    phi = sess.solve_bases(list(r.masks.values()), r.v_basis,
+                                           r.accuracy, out=out)
+                else:
+                    phi = sess.solve_bases(list(r.masks.values()), r.v_basis,
+                                           r.accuracy)
                 result = {i: phi[b] for b, i in enumerate(r.masks)}
                 err = None
             except Exception as e:     # delivered through the future

@@ -39,3 +39,21 @@ def test_result_same_alone_and_in_the_mix():
         assert np.all(alone[i][target[i]] == V)
     lat = srv.latencies()
     assert len(lat) == 6 and all(t >= 0 for row in lat for t in row)
+
+
+def test_device_results_match_host_results():
+    """results="device" returns the same bases as CUDA tensors that stay in
+    HBM (no device-to-host copy in the request)."""
+    import torch
+    from ion_gym_gb300.serve import FieldServer
+    deck = _board(6, (80, 48, 40), 6)
+    host = FieldServer(workers=1)
+    ref = host.submit(deck, V, ACC).result(timeout=300)
+    host.close()
+    dev = FieldServer(workers=1, results="device")
+    got = dev.submit(deck, V, ACC).result(timeout=300)
+    dev.close()
+    assert sorted(got) == sorted(ref)
+    for i in ref:
+        assert isinstance(got[i], torch.Tensor) and got[i].is_cuda
+        assert np.array_equal(got[i].cpu().numpy(), ref[i])
