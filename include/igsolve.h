@@ -201,12 +201,15 @@ int ig_mixed_time_gs(void *handle, int n_problems, int pairs,
  * windowed prolongation vs the per-node gather, [3] = the direction update
  * fused into the operator apply vs the two kernels (direction, L p and the
  * block partials of the inner products), [4] = the four-node restriction
- * of the colour-0 residual vs the per-node one -- each the number of 32-bit words
+ * of the colour-0 residual vs the per-node one, [5] = the CG update of a
+ * refinement step's first iteration (x = alpha p) vs a zeroed x and the
+ * update, and the last iteration's x += alpha p folded into the FP64
+ * update vs the two kernels (potentials and step maxima) -- each the number of 32-bit words
  * that differ over every multigrid level, 0 when bit-identical.
  * Flexible-CG sessions only; no reference counterpart (a self-check of this
  * library's kernel fusion). */
 int ig_mixed_check_fused(void *handle, int n_problems,
-                         long long mismatches[5]);
+                         long long mismatches[6]);
 
 /* ig_cascadic_relres for callers that cannot allocate device memory (no
  * counterpart in the reference).  Some callers may not call cudaMalloc, or

@@ -940,7 +940,8 @@ __device__ __forceinline__ double widen(float d) {
 __global__ void __launch_bounds__(kT)
 k_update64_8(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
              const float* __restrict__ e, SGeo G, unsigned long long* dmax,
-             size_t nstride, size_t pstride) {
+             size_t nstride, size_t pstride, const float* __restrict__ p = nullptr,
+             const double* __restrict__ scal = nullptr) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   unsigned long long key = 0;
   if (t < (G.csz >> 2)) {
@@ -950,8 +951,20 @@ k_update64_8(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
       const int i = (int)fdivu(ij, G.dny);
       const int j = (int)(ij - (uint32_t)i * G.dny.d);
       const int p0 = (i + j) & 1;
-      const float* eb = e + blockIdx.y * pstride + ij * (uint32_t)G.H + (k0 >> 1);
-      const float4 ea = ld4(eb + (size_t)p0 * G.csz), eo = ld4(eb + (size_t)(1 - p0) * G.csz);
+      const float* eb = e ? e + blockIdx.y * pstride + ij * (uint32_t)G.H + (k0 >> 1) : nullptr;
+      float4 ea = e ? ld4(eb + (size_t)p0 * G.csz) : make_float4(0.f, 0.f, 0.f, 0.f);
+      float4 eo = e ? ld4(eb + (size_t)(1 - p0) * G.csz) : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (p) {
+        // the flexible CG's last step x += alpha p, folded in (k_cg_update's
+        // expression; its g half is dead: the residual is recomputed next)
+        const float al = (float)scal[4 * blockIdx.y + 1];
+        const float* pb = p + blockIdx.y * pstride + ij * (uint32_t)G.H + (k0 >> 1);
+        const float4 pa = ld4(pb + (size_t)p0 * G.csz), po = ld4(pb + (size_t)(1 - p0) * G.csz);
+        ea.x = __fmaf_rn(al, pa.x, ea.x); ea.y = __fmaf_rn(al, pa.y, ea.y);
+        ea.z = __fmaf_rn(al, pa.z, ea.z); ea.w = __fmaf_rn(al, pa.w, ea.w);
+        eo.x = __fmaf_rn(al, po.x, eo.x); eo.y = __fmaf_rn(al, po.y, eo.y);
+        eo.z = __fmaf_rn(al, po.z, eo.z); eo.w = __fmaf_rn(al, po.w, eo.w);
+      }
       const float ev[8] = {ea.x, eo.x, ea.y, eo.y, ea.z, eo.z, ea.w, eo.w};
       const uint32_t nat = ij * (uint32_t)G.nz + k0;
       double* q = phi + blockIdx.y * nstride + nat;
@@ -1192,7 +1205,9 @@ k_cg_reduce(const double* __restrict__ part, int nparts, int stride,
   }
 }
 
-// x += alpha p; g += alpha q (float4)
+// x += alpha p; g += alpha q (float4).  FIRST: the step's first iteration,
+// where x is zero: x = alpha p + 0 (the same bits, without reading x).
+template <bool FIRST>
 __global__ void __launch_bounds__(kT)
 k_cg_update(float* __restrict__ x, float* __restrict__ g, const float* __restrict__ p,
             const float* __restrict__ q, const double* __restrict__ scal,
@@ -1201,10 +1216,13 @@ k_cg_update(float* __restrict__ x, float* __restrict__ g, const float* __restric
   if (t >= n / 4) return;  // n: a multiple of 4 (split rows are)
   const float al = (float)scal[4 * blockIdx.y + 1];
   const size_t o = blockIdx.y * pstride + 4 * (size_t)t;
-  float4 xv = ld4(x + o), gv = ld4(g + o);
+  float4 xv = FIRST ? make_float4(0.f, 0.f, 0.f, 0.f) : ld4(x + o);
+  float4 gv = ld4(g + o);
   const float4 pv = ld4(p + o), qv = ld4(q + o);
-  xv.x += al * pv.x; xv.y += al * pv.y; xv.z += al * pv.z; xv.w += al * pv.w;
-  gv.x += al * qv.x; gv.y += al * qv.y; gv.z += al * qv.z; gv.w += al * qv.w;
+  xv.x = __fmaf_rn(al, pv.x, xv.x); xv.y = __fmaf_rn(al, pv.y, xv.y);
+  xv.z = __fmaf_rn(al, pv.z, xv.z); xv.w = __fmaf_rn(al, pv.w, xv.w);
+  gv.x = __fmaf_rn(al, qv.x, gv.x); gv.y = __fmaf_rn(al, qv.y, gv.y);
+  gv.z = __fmaf_rn(al, qv.z, gv.z); gv.w = __fmaf_rn(al, qv.w, gv.w);
   *reinterpret_cast<float4*>(x + o) = xv;
   *reinterpret_cast<float4*>(g + o) = gv;
 }
@@ -1599,17 +1617,24 @@ struct Session {
                                                   f.pstride);
       }
       k_cg_reduce<<<B, kT, 0, s>>>(part.p, 2 * (int)nb4, 2, scal.p, 0);
-      k_cg_update<<<dim3(nblk(n / 4), B), kT, 0, s>>>(xb.p, f.g.p, pcur, qb.p, scal.p, f.pstride,
-                                                     n);
+      // the last iteration's x += alpha p is folded into the FP64 update
+      // below; the first one writes x = alpha p (no zeroing pass)
+      if (it == 0 && cg_iters > 1)
+        k_cg_update<true><<<dim3(nblk(n / 4), B), kT, 0, s>>>(xb.p, f.g.p, pcur, qb.p, scal.p,
+                                                             f.pstride, n);
+      else if (it + 1 < cg_iters)
+        k_cg_update<false><<<dim3(nblk(n / 4), B), kT, 0, s>>>(xb.p, f.g.p, pcur, qb.p, scal.p,
+                                                              f.pstride, n);
     }
+    const dim3 gn(nblk(f.G.n), B);
+    MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
+    // phi += x + alpha p (x absent when the step has one iteration)
+    k_update64_8<<<dim3(nblk(f.G.csz / 4), B), kT, 0, s>>>(
+        phi.p, fixed.p, cg_iters > 1 ? xb.p : nullptr, f.G, dmax.p, f.G.n, f.pstride, pcur,
+        scal.p);
     // the next step (a replay of this graph) starts from pb
     if (pcur != pb.p)
       MK(cudaMemcpyAsync(pb.p, pcur, f.pstride * B * 4, cudaMemcpyDeviceToDevice, s));
-    const dim3 gn(nblk(f.G.n), B);
-    MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
-    k_update64_8<<<dim3(nblk(f.G.csz / 4), B), kT, 0, s>>>(phi.p, fixed.p, xb.p, f.G, dmax.p,
-                                                         f.G.n, f.pstride);
-    MK(cudaMemsetAsync(xb.p, 0, f.pstride * B * 4, s));
     k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, f.G.n, f.pstride);
   }
 
@@ -1644,7 +1669,10 @@ struct Session {
   }
 
   long launches_per_step() const {
-    if (method == 1) return 2 + cg_iters * (cycle_launches(0, true) + (fuse_dir() ? 5 : 6));
+    // per iteration: dot, two reductions, direction + L p (one launch when
+    // fused) and, on all but the last, the CG update; then update64, resid64
+    if (method == 1)
+      return 2 + cg_iters * (cycle_launches(0, true) + (fuse_dir() ? 4 : 5)) + (cg_iters - 1);
     long n = 2;
     for (int v = 0; v < vcycles; v++) n += cycle_launches(0, v == 0);
     return n;
@@ -1811,7 +1839,7 @@ int ig_mixed_time_gs(void* handle, int n_problems, int pairs, double* ms_per_lau
   }
 }
 
-int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[5]) {
+int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[6]) {
   set_last_error("");
   Session* S = static_cast<Session*>(handle);
   if (!S || !mismatches || n_problems < 1 || n_problems > S->bmax || S->method != 1 ||
@@ -1824,8 +1852,8 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[5]) 
     const int B = n_problems;
     cudaStream_t s = S->s;
     Buf<unsigned long long> bad;
-    bad.alloc(5, s);
-    MK(cudaMemsetAsync(bad.p, 0, 40, s));
+    bad.alloc(6, s);
+    MK(cudaMemsetAsync(bad.p, 0, 48, s));
     long launches = 0;
     auto diff = [&](const void* a, const void* b, size_t words, int slot) {
       k_count_diff<<<dim3((unsigned)((words + kT - 1) / kT), 1), kT, 0, s>>>(
@@ -1896,11 +1924,45 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[5]) 
       diff(S->part.p, part2.p, 2 * nparts, 3);
       launches += 3;
     }
-    unsigned long long h[5] = {0, 0, 0, 0, 0};
-    MK(cudaMemcpyAsync(h, bad.p, 40, cudaMemcpyDeviceToHost, s));
+    // the CG update of a step's first iteration (x = alpha p) against a
+    // zeroed x and the update, and the last iteration's x += alpha p folded
+    // into the FP64 update against the two kernels (potentials and maxima)
+    {
+      MLevel& f = S->lv[0];
+      const size_t words = f.pstride * B;
+      const uint32_t n = (uint32_t)f.pstride;
+      const dim3 gu(nblk(n / 4), B), g8(nblk(f.G.csz / 4), B);
+      float* x = S->xb.p;
+      float* p = S->pb.p;
+      MK(cudaMemsetAsync(x, 0, words * 4, s));
+      k_cg_update<false><<<gu, kT, 0, s>>>(x, f.g.p, p, S->qb.p, S->scal.p, f.pstride, n);
+      MK(cudaMemcpyAsync(scrA, x, words * 4, cudaMemcpyDeviceToDevice, s));
+      k_cg_update<true><<<gu, kT, 0, s>>>(x, f.g.p, p, S->qb.p, S->scal.p, f.pstride, n);
+      diff(x, scrA, words, 5);
+      const size_t nphi = f.G.n * (size_t)B;
+      Buf<double> phi0, phi1;
+      phi0.alloc(nphi, s);
+      phi1.alloc(nphi, s);
+      Buf<unsigned long long> dm;
+      dm.alloc(2 * (size_t)B, s);
+      MK(cudaMemsetAsync(dm.p, 0, 16 * (size_t)B, s));
+      MK(cudaMemcpyAsync(phi0.p, S->phi.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
+      MK(cudaMemcpyAsync(scrB, x, words * 4, cudaMemcpyDeviceToDevice, s));   // x kept
+      k_cg_update<false><<<gu, kT, 0, s>>>(x, f.g.p, p, S->qb.p, S->scal.p, f.pstride, n);
+      k_update64_8<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, x, f.G, dm.p, f.G.n, f.pstride);
+      MK(cudaMemcpyAsync(phi1.p, S->phi.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
+      MK(cudaMemcpyAsync(S->phi.p, phi0.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
+      k_update64_8<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, scrB, f.G, dm.p + B, f.G.n, f.pstride,
+                                     p, S->scal.p);
+      diff(S->phi.p, phi1.p, 2 * nphi, 5);
+      diff(dm.p, dm.p + B, 2 * (size_t)B, 5);
+      launches += 6;
+    }
+    unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
+    MK(cudaMemcpyAsync(h, bad.p, 48, cudaMemcpyDeviceToHost, s));
     MK(cudaStreamSynchronize(s));
     g_mixed_launches.fetch_add(launches);
-    for (int q = 0; q < 5; q++) mismatches[q] = (long long)h[q];
+    for (int q = 0; q < 6; q++) mismatches[q] = (long long)h[q];
     return (int)IG_OK;
   } catch (int code) {
     return code;

@@ -82,8 +82,10 @@ def test_fused_kernels_are_bit_identical(shape, seed):
     levels reach size-1 axes (the per-node prolongation takes over there):
     the first Gauss-Seidel pair from a zero correction, the float4 colour-0
     residual, the windowed prolongation, the direction update fused into
-    the operator apply (direction, L p and the inner-product partials), and
-    the four-node restriction of the colour-0 residual."""
+    the operator apply (direction, L p and the inner-product partials), the
+    four-node restriction of the colour-0 residual, the first CG update of a
+    refinement step written without reading x, and the last one folded
+    into the FP64 update."""
     import ctypes
     from ion_gym_gb300 import _lib
     from ion_gym_gb300.physics.mixed import MixedSession
@@ -94,7 +96,7 @@ def test_fused_kernels_are_bit_identical(shape, seed):
     rings = [masks[i] for i in sorted(masks)]
     with MixedSession(metal, len(rings)) as s:
         s.solve_bases(rings, V, ACC)
-        bad = (ctypes.c_longlong * 5)(-1, -1, -1, -1, -1)
+        bad = (ctypes.c_longlong * 6)(-1, -1, -1, -1, -1, -1)
         st = _lib.lib().ig_mixed_check_fused(s._h, len(rings), bad)
         _lib.check(st, "ig_mixed_check_fused")
-    assert list(bad) == [0, 0, 0, 0, 0]
+    assert list(bad) == [0, 0, 0, 0, 0, 0]
