@@ -7,13 +7,16 @@
 //
 //   phi64 <- Dirichlet values                                  (FP64, HBM)
 //   repeat:  g32 = -(float) r64(phi64)      r64: the reference's fine-level
-//                                           residual (multigrid3d.py:305-354)
-//                                           in FP64, 0 at metal
-//            e32 = m V-cycles on  A e = g   (FP32, A e = sum(nbr e) - 6 e,
-//                                           block-ANY coarse masks, full
-//                                           weighting x4, trilinear
-//                                           prolongation, red-black GS)
-//            phi64 += e32;  stop when max|e32| < acc   (per basis)
+//                                           residual (multigrid3d.py:305-354),
+//                                           formed exactly, 0 at metal
+//            x32 = cg_iters iterations of flexible CG on A x = g (FP32,
+//                  A x = sum(nbr x) - 6 x), each preconditioned by one
+//                  multigrid V-cycle (block-ANY coarse masks, 13-point
+//                  restriction of the colour-0 residual, trilinear
+//                  prolongation, red-black Gauss-Seidel, one-CTA bottom)
+//            phi64 += x32;  stop when the step and its geometric tail
+//                           estimate are below acc     (per problem)
+//   (method 0 replaces the CG by `vcycles` plain V-cycles per step)
 //
 // FP32 data live in a red-black split layout: colour c of row (i, j) holds
 // nodes k = 2m + ((i+j+c) & 1) at index m, so one colour's update reads the
@@ -23,9 +26,9 @@
 // update in FP32 against 26 for the natural layout.
 //
 // Batching: blockIdx.y is the problem index; masks are shared, per-problem
-// arrays are strided.  The whole refinement step (residual, V-cycles,
-// update) is captured once into a CUDA graph and replayed; the host reads
-// only the B correction maxima per step.
+// arrays are strided.  The whole refinement step (CG iterations, FP64
+// update, residual) is captured once into a CUDA graph and replayed; the
+// host reads only the B step maxima per step.
 #include <algorithm>
 #include <atomic>
 #include <cmath>
