@@ -111,10 +111,11 @@ def dist():
     return replicas.world()
 
 
-def cpu_sample(fixed, seconds=15.0, max_pairs=400):
+def cpu_sample(fixed, seconds=15.0, max_pairs=20000):
     """Time red-black pairs of the reference sweep (oracle C restatement,
     all host threads, theta read as ones as the reference does) on the fine
-    grid.  Returns (GLUP/s, pairs timed, seconds, threads)."""
+    grid for about `seconds` (max_pairs only bounds a very fast host).
+    Returns (GLUP/s, pairs timed, seconds, threads)."""
     from oracle import port
     shape = fixed.shape
     phi = np.zeros(shape)
