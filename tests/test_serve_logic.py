@@ -91,3 +91,9 @@ def test_schedule_and_percentiles():
     assert 800 < len(t) < 1200 and all(np.diff(t) > 0)
     assert percentile([1, 2, 3, 4], 50) == 2.5
     assert percentile([], 99) is None
+
+
+def test_unknown_results_kind_is_refused():
+    with pytest.raises(ValueError, match="results"):
+        FieldServer(workers=1, hbm_budget=100, device=None,
+                    session_factory=FakeSession, results="disk")
