@@ -140,14 +140,15 @@ def lups_per_solve(level_pairs):
     return sum(int(np.prod(s)) * p for s, p in zip(shapes, level_pairs))
 
 
-def load_profile_traffic(name="sweep_f64_quad257.md"):
-    """dram bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/<name>: its `dram_bytes_per_launch:` line), or None."""
+def load_profile_traffic(name="sweep_f64_quad257.md", key="dram_bytes_per_launch"):
+    """A figure of the dominant kernel from the committed ncu summary
+    (profiles/<name>: its `<key>:` line -- dram bytes per launch by
+    default), or None."""
     p = os.path.join(ROOT, "profiles", name)
     if not os.path.exists(p):
         return None
     for line in open(p):
-        if line.startswith("dram_bytes_per_launch:"):
+        if line.startswith(key + ":"):
             try:
                 return float(line.split(":", 1)[1].split()[0])
             except ValueError:
@@ -256,6 +257,10 @@ def run_ours(a):
                      "frac": (achieved / peak) if peak else None,
                      "traffic": traffic,
                      "kernel": "k_sweep<kPlain> (FP64 red-black sweep)",
+                     # the kernel is bound by GB300's FP64 pipe, not HBM:
+                     # its busy fraction from the same ncu summary
+                     "fp64_pipe_busy_ncu": load_profile_traffic(
+                         key="fp64_pipe_busy_frac"),
                      "avg_launch_us": 1e3 * ms.value / max(nl.value, 1),
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"
                      if peak else None},
