@@ -1003,11 +1003,35 @@ k_update64_8(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
              const float* __restrict__ e, SGeo G, unsigned long long* dmax,
              size_t nstride, size_t pstride, const float* __restrict__ p = nullptr,
              const double* __restrict__ scal = nullptr) {
-  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  // The block's groups cover one contiguous natural range [n_lo, n_hi) (a
+  // row's valid groups are consecutive and the next row starts where it
+  // ends; groups past a row's end cover nothing), at most 8 kT nodes: the
+  // potentials and masks of that range go through shared memory, so global
+  // loads and stores are coalesced whole rows instead of 64-byte pieces per
+  // thread.
+  __shared__ double sphi[kT * 8];
+  __shared__ uint8_t sfix[kT * 8];
+  const uint32_t ngroups = G.csz >> 2;
+  const uint32_t H4 = G.dH4.d;
+  const uint32_t t0 = blockIdx.x * kT;
+  const uint32_t t1 = min(t0 + kT, ngroups) - 1;
+  const uint32_t ij0 = fdivu(t0, G.dH4), ij1 = fdivu(t1, G.dH4);
+  const uint32_t k00 = 8 * (t0 - ij0 * H4), k01 = 8 * (t1 - ij1 * H4);
+  const uint32_t nz = (uint32_t)G.nz;
+  const uint32_t n_lo = k00 < nz ? ij0 * nz + k00 : (ij0 + 1) * nz;
+  const uint32_t n_hi = k01 < nz ? min(ij1 * nz + k01 + 8, (ij1 + 1) * nz) : (ij1 + 1) * nz;
+  const uint32_t span = n_hi > n_lo ? n_hi - n_lo : 0;
+  double* P = phi + blockIdx.y * nstride;
+  for (uint32_t q = threadIdx.x; q < span; q += kT) {
+    sphi[q] = P[n_lo + q];
+    sfix[q] = fixed[n_lo + q];
+  }
+  __syncthreads();
+  const uint32_t t = t0 + threadIdx.x;
   unsigned long long key = 0;
-  if (t < (G.csz >> 2)) {
+  if (t < ngroups) {
     const uint32_t ij = fdivu(t, G.dH4);
-    const int k0 = 8 * (int)(t - ij * G.dH4.d);
+    const int k0 = 8 * (int)(t - ij * H4);
     if (k0 < G.nz) {
       const int i = (int)fdivu(ij, G.dny);
       const int j = (int)(ij - (uint32_t)i * G.dny.d);
@@ -1027,13 +1051,12 @@ k_update64_8(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
         eo.z = __fmaf_rn(al, po.z, eo.z); eo.w = __fmaf_rn(al, po.w, eo.w);
       }
       const float ev[8] = {ea.x, eo.x, ea.y, eo.y, ea.z, eo.z, ea.w, eo.w};
-      const uint32_t nat = ij * (uint32_t)G.nz + k0;
-      double* q = phi + blockIdx.y * nstride + nat;
+      const uint32_t off = ij * nz + (uint32_t)k0 - n_lo;
 #pragma unroll
       for (int u = 0; u < 8; u++) {
-        if (k0 + u >= G.nz || fixed[nat + u]) continue;
+        if (k0 + u >= G.nz || sfix[off + u]) continue;
         const double dd = widen(ev[u]);
-        q[u] = q[u] + dd;
+        sphi[off + u] = sphi[off + u] + dd;
         unsigned long long kk =
             static_cast<unsigned long long>(__double_as_longlong(dd)) & 0x7fffffffffffffffULL;
         if (kk > 0x7ff0000000000000ULL) kk = 0x7ff0000000000000ULL;  // NaN: never converged
@@ -1041,6 +1064,8 @@ k_update64_8(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
       }
     }
   }
+  __syncthreads();
+  for (uint32_t q = threadIdx.x; q < span; q += kT) P[n_lo + q] = sphi[q];
   block_max_to(key, dmax + blockIdx.y);
 }
 
