@@ -207,3 +207,15 @@ def test_concurrent_basis_door_keeps_the_serial_order(monkeypatch, capsys):
     assert list(out) == [2, 3, 5]
     for k, phi in out.items():
         assert phi.shape == shape and np.all(phi == k)
+
+
+def test_empty_basis_deck_fails_like_the_reference():
+    """An empty {index: mask} deck: the reference's basis doors take the
+    first mask's shape with next(iter(...)) and raise StopIteration before
+    any solve (solver3d.py:296-320, multigrid3d.py:233-246); the drop-ins
+    do the same, before touching the GPU."""
+    from ion_gym_gb300.physics import solver3d, multigrid3d
+    with pytest.raises(StopIteration):
+        solver3d.solve_bases({})
+    with pytest.raises(StopIteration):
+        multigrid3d.solve_bases_mg({})
