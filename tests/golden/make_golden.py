@@ -30,6 +30,8 @@ Fixture files:
                export_field_bundle / import_field_bundle /
                read_field_arrays on a small 3-D entry: the key, every bundle
                member, the spec JSON written beside it and the refusals.
+  pasurf.npz   solver3d.fractions_from_pa_surf on synthetic surface-fraction
+               sidecars (the sidecar bytes, grid, metal and theta).
 """
 import argparse
 import json
@@ -375,6 +377,52 @@ def theta_cases(S):
     out["theta/2/mirror"] = np.array([True, True, False])
     out["theta/2/th"] = S.fractions_from_scene(sc3, mq,
                                                mirror=(True, True, False))
+    return out
+
+
+def pasurf_cases(S):
+    """solver3d.fractions_from_pa_surf on synthetic surface-fraction
+    sidecars: a header, XOFF / YOFF / ZOFF chunks of (u64 flat index with x
+    fastest, f64 fraction) records at vacuum and metal nodes (metal records
+    set the -leg of the vacuum node above; records whose node above is metal
+    or off the grid are dropped), fractions below the 1e-3 clamp, indices
+    past the grid, terminator records, and an empty chunk."""
+    import tempfile
+    out = {}
+    rng = np.random.default_rng(4242)
+    for case, shape in enumerate([(9, 7, 6), (5, 8, 1), (12, 4, 5)]):
+        nx, ny, nz = shape
+        n = nx * ny * nz
+        metal = rng.random(shape) < 0.3
+        chunks = [b"SIMEXP\x00\x01" + bytes(8)]
+        for tag in (b"XOFF", b"YOFF", b"ZOFF"):
+            if tag == b"ZOFF" and case == 1:
+                chunks.append(tag)              # empty chunk
+                continue
+            m = int(rng.integers(10, 40))
+            idx = rng.integers(0, n, m).astype("<u8")
+            f = rng.random(m)
+            f[:3] = [0.0, 5e-4, 1.0]            # clamp and edge fractions
+            rec = np.empty(m + 2, dtype=[("idx", "<u8"), ("f", "<f8")])
+            rec["idx"][:m] = idx
+            rec["f"][:m] = f
+            rec["idx"][m] = n + 7                # past the grid
+            rec["f"][m] = 0.5
+            rec["idx"][m + 1] = 0xFFFFFFFF00000000  # terminator record
+            rec["f"][m + 1] = 0.0
+            chunks.append(tag + rec.tobytes())
+        raw = b"".join(chunks)
+        with tempfile.NamedTemporaryFile(suffix=".surf", delete=False) as fh:
+            fh.write(raw)
+            path = fh.name
+        try:
+            th = S.fractions_from_pa_surf(path, shape, metal)
+        finally:
+            os.unlink(path)
+        out[f"pasurf/{case}/raw"] = np.frombuffer(raw, np.uint8).copy()
+        out[f"pasurf/{case}/shape"] = np.array(shape)
+        out[f"pasurf/{case}/metal"] = metal.astype(np.uint8)
+        out[f"pasurf/{case}/th"] = th
     return out
 
 
@@ -807,7 +855,8 @@ def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--out", default=os.path.dirname(os.path.abspath(__file__)))
     ap.add_argument("--only", choices=["kernels", "drivers", "theta", "cache",
-                                       "raster", "field", "bundle", "shapes"],
+                                       "raster", "field", "bundle", "shapes",
+                                       "pasurf"],
                     default=None)
     a = ap.parse_args()
     import ion_gym.physics.solver3d as S
@@ -842,6 +891,9 @@ def main():
     if a.only in (None, "bundle"):
         np.savez_compressed(os.path.join(a.out, "bundle.npz"), **bundle_cases())
         print("bundle.npz written")
+    if a.only in (None, "pasurf"):
+        np.savez_compressed(os.path.join(a.out, "pasurf.npz"), **pasurf_cases(S))
+        print("pasurf.npz written")
 
 
 if __name__ == "__main__":

@@ -219,3 +219,25 @@ def test_empty_basis_deck_fails_like_the_reference():
         solver3d.solve_bases({})
     with pytest.raises(StopIteration):
         multigrid3d.solve_bases_mg({})
+
+
+def test_pa_surf_sidecar_matches_reference(tmp_path):
+    """fractions_from_pa_surf (solver3d.py:323-363) decodes the reference's
+    theta, bit for bit, from synthetic sidecars recorded with the
+    reference's reader (tests/golden/pasurf.npz): vacuum and metal records,
+    clamped fractions, records past the grid, terminators, an empty chunk."""
+    import os
+    from ion_gym_gb300.physics import solver3d
+    z = np.load(os.path.join(os.path.dirname(__file__), "golden", "pasurf.npz"))
+    cases = sorted({k.split("/")[1] for k in z.files})
+    assert len(cases) == 3
+    for c in cases:
+        path = tmp_path / f"case{c}.surf"
+        path.write_bytes(z[f"pasurf/{c}/raw"].tobytes())
+        shape = tuple(int(s) for s in z[f"pasurf/{c}/shape"])
+        th = solver3d.fractions_from_pa_surf(str(path), shape,
+                                             z[f"pasurf/{c}/metal"].astype(bool))
+        want = z[f"pasurf/{c}/th"]
+        assert th.dtype == want.dtype and th.shape == want.shape
+        assert np.array_equal(th.view(np.uint32), want.view(np.uint32))
+        assert (want < 1).sum() > 5
