@@ -235,3 +235,36 @@ def test_torch_tensors_in_place(dev):
     db = port.sweep(b, fixed, np.ones((6, 20, 21, 22), np.float32), 1.5, 0, True)
     assert t.data_ptr() == ptr and d == db
     assert same_bits(t.cpu().numpy(), b)
+
+
+def test_residual_field_and_attribute_difference_match_oracle():
+    """solver3d.residual_field and attribute_difference (solver3d.py:420-444)
+    against the oracle's restatement of the same audit and error-equation
+    loop, bit for bit, with theta given."""
+    from ion_gym_gb300.physics import solver3d as S
+    rng = np.random.default_rng(31)
+    shape = (14, 11, 9)
+    fixed = np.zeros(shape, bool)
+    fixed[0] = fixed[-1] = True
+    fixed[:, 0] = fixed[:, -1] = True
+    fixed[:, :, 0] = fixed[:, :, -1] = True
+    fixed[5:8, 4:7, 3:6] = True
+    val = np.where(fixed, rng.uniform(-1.0, 1.0, shape), 0.0)
+    theta = np.where(rng.random((6,) + shape) < 0.7, 1.0,
+                     rng.uniform(0.2, 1.0, (6,) + shape)).astype(np.float32)
+    ref = np.where(fixed, val, rng.uniform(-1.0, 1.0, shape))
+    phi = np.where(fixed, val, ref + rng.normal(0.0, 1e-6, shape))
+    r = S.residual_field(ref, fixed, theta)
+    ro = port.residual_audit(ref, fixed, theta)
+    assert same_bits(r, ro)
+    e, rest = S.attribute_difference(ref, phi, fixed, theta, tol=1e-9,
+                                     max_sweeps=400)
+    eo = np.zeros_like(ref)
+    om = 2.0 / (1.0 + np.sin(np.pi / (max(shape) + 1)))
+    for _ in range(400):
+        d = max(port.err_sweep(eo, fixed, theta, -ro, om, 0),
+                port.err_sweep(eo, fixed, theta, -ro, om, 1))
+        if d < 1e-9:
+            break
+    assert same_bits(e, eo)
+    assert same_bits(rest, (ref - phi) - eo)
