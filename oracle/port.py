@@ -286,12 +286,7 @@ def solve3d_mg(fixed, val, theta=None, mirror=(False, False, False), tol=1e-6,
     """multigrid3d.solve3d_mg (multigrid3d.py:175-230), the cascadic scheme.
     omega (not in the reference signature) fixes the SOR factor on every
     level; None keeps the reference's per-level optimum."""
-    levels = [(np.asarray(fixed, bool), np.asarray(val, np.float64))]
-    while len(levels) < max_levels:
-        f, v = levels[-1]
-        if min(f.shape) <= min_coarse or min((s + 1) // 2 for s in f.shape) < 3:
-            break
-        levels.append(coarsen_mask(f, v))
+    levels = cascadic_levels(fixed, val, min_coarse, max_levels)
     fc, vc = levels[-1]
     phic, _, _ = solve3d(fc, vc, theta=None, tol=tol, max_sweeps=max_sweeps,
                          stencil=stencil, omega=omega)
@@ -308,6 +303,92 @@ def solve3d_mg(fixed, val, theta=None, mirror=(False, False, False), tol=1e-6,
         p0[f] = v[f]
     return solve3d(f, v, theta=theta, tol=tol, max_sweeps=max_sweeps,
                    phi0=p0, stencil=stencil, omega=omega)
+
+
+def cascadic_levels(fixed, val, min_coarse=9, max_levels=8):
+    """The cascadic hierarchy of solve3d_mg (multigrid3d.py:188-194): the
+    fine (fixed, val) and its _coarsen_mask levels, fine first."""
+    levels = [(np.asarray(fixed, bool), np.asarray(val, np.float64))]
+    while len(levels) < max(1, max_levels):
+        f, v = levels[-1]
+        if min(f.shape) <= min_coarse or min((s + 1) // 2 for s in f.shape) < 3:
+            break
+        levels.append(coarsen_mask(f, v))
+    return levels
+
+
+def solve3d_cascadic_relres(fixed, val, rel_tol=1e-10, omega=1.85,
+                            max_levels=4, min_coarse=9, check_every=20,
+                            level_tol_factor=30.0, max_sweeps=200000,
+                            on_level=None):
+    """The residual-stopped cascadic solve of the 257^3 quadrupole workload
+    (no reference driver: the reference's cascadic solve3d_mg,
+    multigrid3d.py:175-230, stops each level on the max |update| of a sweep
+    pair; this rule stops it on a relative residual instead).
+
+    Built from the reference's pieces: the solve3d_mg hierarchy
+    (_coarsen_mask, multigrid3d.py:85-135, at most max_levels levels), the
+    coarsest level started from its Dirichlet values with zeros elsewhere,
+    each finer level from _prolongate (multigrid3d.py:138-171) of the level
+    below with its Dirichlet values reset, red-black _sweep pairs
+    (solver3d.py:131-198, theta None read as ones) at omega[L] on level L
+    (fine = 0), and the relative residual max|r| / max|r(phi_D)| with r from
+    multigrid3d._residual (multigrid3d.py:305-354) and phi_D the level's
+    Dirichlet values with zeros elsewhere, checked before the first pair and
+    after every `check_every` pairs.  The coarsest and fine levels stop below
+    rel_tol, intermediate levels below rel_tol * level_tol_factor (the
+    reference's level_tol_factor); max_sweeps caps each level's pairs, and a
+    coarse level that reaches the cap hands its iterate on (only the fine
+    level's cap raises SolveNotConverged).
+
+    Returns (phi, fine pairs, fine relative residual, pairs on all levels,
+    per-level pair counts coarsest first).  on_level(L, shape, pairs, rr),
+    when given, is called after each level."""
+    levels = cascadic_levels(fixed, val, min_coarse, max_levels)
+    nl = len(levels)
+    om = np.broadcast_to(np.asarray(omega, np.float64), (nl,))
+    ones = None
+    cur = None
+    total = 0
+    per_level = []
+    phi = rr = pairs = None
+    for L in range(nl - 1, -1, -1):
+        f, v = levels[L]
+        if ones is None or ones.shape[1:] != f.shape:
+            ones = np.ones((6,) + f.shape, np.float32)
+        r = np.empty(f.shape)
+        phid = np.zeros(f.shape)
+        phid[f] = v[f]
+        residual(phid, f, ones, True, r)
+        bnorm = float(np.abs(r).max())
+        if L < nl - 1:
+            phi = prolongate(cur, f.shape)
+            phi[f] = v[f]
+        else:
+            phi = phid
+        ltol = rel_tol if L in (0, nl - 1) else rel_tol * level_tol_factor
+        pairs = 0
+        while True:
+            residual(phi, f, ones, True, r)
+            rmax = float(np.abs(r).max())
+            rr = rmax / bnorm if bnorm > 0 else rmax
+            if rr < ltol or pairs >= max_sweeps:
+                break
+            chunk = min(check_every, max_sweeps - pairs)
+            for _ in range(chunk):
+                sweep(phi, f, ones, float(om[L]), 0, True)
+                sweep(phi, f, ones, float(om[L]), 1, True)
+            pairs += chunk
+        total += pairs
+        per_level.append(pairs)
+        if on_level is not None:
+            on_level(L, f.shape, pairs, rr)
+        if L == 0 and not rr < ltol:
+            raise SolveNotConverged(
+                f"cascadic solve stopped at {max_sweeps} sweeps with relative "
+                f"residual {rr:.3e} vs {rel_tol:.1e}")
+        cur = phi
+    return phi, pairs, rr, total, per_level
 
 
 def _solve_err(fixed, f, rel_tol=0.02, max_cycles=30, nu1=2, nu2=2,

@@ -100,3 +100,25 @@ def test_fused_kernels_are_bit_identical(shape, seed):
         st = _lib.lib().ig_mixed_check_fused(s._h, len(rings), bad)
         _lib.check(st, "ig_mixed_check_fused")
     assert list(bad) == [0, 0, 0, 0, 0, 0]
+
+
+@pytest.mark.parametrize("seed,side,n_el", [(1000, 33, 5), (1001, 65, 12),
+                                            (1002, 97, 3), (1003, 65, 16)])
+def test_uneven_batch_decks_reach_fp64_accuracy(seed, side, n_el):
+    """Decks of the uneven-batch workload (random spheres, cylinders and
+    plates in a grounded box, voltages U(-100, 100) V) solved by a mixed
+    session as the batch solves them: within 1e-9 of each deck's voltage
+    span of the FP64 drop-in V-cycle run to 1e-13 of the span."""
+    from ion_gym_gb300.physics import multigrid3d as M
+    from ion_gym_gb300.physics.mixed import MixedSession
+    from ion_gym_gb300.workloads import random_deck
+    fixed, val = random_deck(seed, side, n_el)
+    span = max(float(val.max() - val.min()), 1.0)
+    ref = M.solve3d_vmg(fixed, val, tol=1e-13 * span, max_cycles=400,
+                        accept_stagnation=True)[0]
+    with MixedSession(fixed, 1) as s:
+        got = s.solve_values(val, ACC, span=span)[0]
+        steps = s.last_steps
+    err = np.abs(got - ref).max() / span
+    assert err <= ACC, (err, steps)
+    assert np.array_equal(got[fixed], val[fixed])

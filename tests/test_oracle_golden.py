@@ -156,3 +156,39 @@ def test_basis_doors(drivers_golden):
     assert sorted(out) == list(m["keys"])
     for i in (1, 2):
         assert same_bits(out[i], m[f"b{i}"])
+
+
+def test_relres_driver_restates_its_rule():
+    """The oracle's residual-stopped cascadic driver (the quadrupole
+    workload's rule; no reference driver to replay) is built from the pinned
+    kernels above and the hierarchy of the pinned solve3d_mg; its own rule
+    is checked here: the returned relative residual is max|r| / max|r(phi_D)|
+    of the returned potential, every level's pairs are whole residual-check
+    chunks, the level shapes are solve3d_mg's, and a tolerance already met
+    runs no pair at all."""
+    from ion_gym_gb300.physics.multigrid3d import cascadic_shapes
+    n = 33
+    i, j, k = np.meshgrid(*[np.arange(n, dtype=float)] * 3, indexing="ij")
+    fixed = np.zeros((n, n, n), bool)
+    fixed[0] = fixed[-1] = True
+    fixed[:, 0] = fixed[:, -1] = True
+    fixed[:, :, 0] = fixed[:, :, -1] = True
+    s = (i - 16) ** 2 + (j - 16) ** 2 + (k - 16) ** 2 <= 25
+    fixed |= s
+    val = np.where(s, 1.0, 0.0)
+    seen = []
+    phi, fine, rr, tot, per = port.solve3d_cascadic_relres(
+        fixed, val, rel_tol=1e-9, omega=1.8, max_levels=3, check_every=6,
+        on_level=lambda L, shape, p, r: seen.append(shape))
+    assert [tuple(x) for x in seen[::-1]] == cascadic_shapes((n,) * 3, 9, 3)
+    assert all(p % 6 == 0 for p in per) and sum(per) == tot and per[-1] == fine
+    ones = np.ones((6, n, n, n), np.float32)
+    r = np.empty_like(phi)
+    port.residual(phi, fixed, ones, True, r)
+    phid = np.where(fixed, val, 0.0)
+    r0 = np.empty_like(phi)
+    port.residual(phid, fixed, ones, True, r0)
+    assert rr == float(np.abs(r).max()) / float(np.abs(r0).max()) and rr < 1e-9
+    assert np.array_equal(phi[fixed], val[fixed])
+    _, fine0, _, tot0, _ = port.solve3d_cascadic_relres(fixed, val, rel_tol=2.0)
+    assert fine0 == 0 and tot0 == 0
