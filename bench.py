@@ -15,9 +15,12 @@ L2 flush is needed between steps.
 Prints one JSON line.  `value` is solves/s with the inputs resident in HBM;
 `e2e` is the same solve through the public API from pinned host buffers
 (host->device copies of mask and Dirichlet values, device->host copy of phi
-inside the timed region).  `--impl reference` times the CPU restatement of
-the reference's sweep (oracle/, all host threads) on a bounded sample of the
-same workload.
+inside the timed region).  The line also carries the same quadrupole through
+the mixed-precision session (`mixed`), the ring-stack basis batch of BASELINE
+config 3 (`rings`: mixed against the FP64 drop-in basis door) and one
+complete CPU solve (`cpu_baseline`).  `--impl reference` times the oracle's
+restatement of the reference's CPU path (oracle/, all host threads), each
+step one complete solve of the same workload.
 """
 import argparse
 import json
@@ -135,9 +138,43 @@ def cpu_sample(fixed, seconds=15.0, max_pairs=20000):
     return n * pairs / el / 1e9, pairs, el, port.num_threads()
 
 
+def cpu_full_solve(fixed, val):
+    """One complete solve of the workload by the oracle's restatement of the
+    driver (oracle.port.solve3d_cascadic_relres: the reference's sweep,
+    residual, coarsening and prolongation in C on all host threads, theta
+    read as ones as the reference does).  Returns (seconds, fine pairs,
+    fine relative residual, pairs on all levels, LUPs, threads)."""
+    from oracle import port
+    t0 = time.perf_counter()
+    _, fine, rr, tot, per = port.solve3d_cascadic_relres(
+        fixed, val, rel_tol=REL_TOL, omega=OMEGA, max_levels=LEVELS,
+        min_coarse=9, check_every=CHECK_EVERY)
+    secs = time.perf_counter() - t0
+    return secs, fine, rr, tot, lups_per_solve(per[::-1]), port.num_threads()
+
+
 def lups_per_solve(level_pairs):
+    """LUPs of one solve from its pairs per level (fine first)."""
     shapes = level_shapes()
     return sum(int(np.prod(s)) * p for s, p in zip(shapes, level_pairs))
+
+
+def workload_config(ws=1):
+    return {"workload": WORKLOAD, "grid": [N_SIDE] * 3,
+            "levels": [list(s) for s in level_shapes()],
+            "omega": OMEGA, "rel_tol": REL_TOL,
+            "check_every_pairs": CHECK_EVERY,
+            "parallelism": f"replicas{ws}" if ws > 1 else "single",
+            "l2": "inputs larger than L2 (153 MB resident > 129 MB)"}
+
+
+def fp64_tight(fixed, val, span):
+    """The FP64 drop-in V-cycle (bit-identical to the reference's
+    solve3d_vmg) run to a cycle delta of 1e-13 of the span: the reference
+    solution the mixed results are measured against."""
+    from ion_gym_gb300.physics import multigrid3d as MG
+    return MG.solve3d_vmg(fixed, val, tol=1e-13 * span, max_cycles=400,
+                          accept_stagnation=True)[0]
 
 
 def load_profile_traffic(name="sweep_f64_quad257.md", key="dram_bytes_per_launch"):
@@ -239,14 +276,11 @@ def run_ours(a):
         "ms_per_step": 1e3 * el / a.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64",
         "data": "synthetic (seeded geometry of the named workload)",
-        "config": {"workload": WORKLOAD, "grid": [N_SIDE] * 3,
-                   "levels": [list(s) for s in level_shapes()],
-                   "omega": OMEGA, "rel_tol": REL_TOL,
-                   "check_every_pairs": CHECK_EVERY,
-                   "parallelism": f"replicas{ws}" if ws > 1 else "single",
-                   "l2": "inputs larger than L2 (153 MB resident > 129 MB)"},
+        "config": workload_config(ws),
         "glup_s": glups,
         "lups_per_solve": lups,
+        "lups_source": "FP64 sweep launches of the timed solves, counted by "
+                       "the library's profiler",
         "fine_pairs": fine_pairs, "total_pairs": total_pairs,
         "fine_relres": relres,
         "e2e": {"value": ws * a.steps / el_e2e, "unit": "solves/s",
@@ -256,11 +290,15 @@ def run_ours(a):
                      "unit": "GB/s",
                      "frac": (achieved / peak) if peak else None,
                      "traffic": traffic,
+                     "traffic_source": "ncu dram__bytes per fine-level launch "
+                     "from the committed capture profiles/sweep_f64_quad257.md "
+                     "(not measured in this run)" if traffic else None,
                      "kernel": "k_sweep<kPlain> (FP64 red-black sweep)",
                      # the kernel is bound by GB300's FP64 pipe, not HBM:
                      # its busy fraction from the same ncu summary
                      "fp64_pipe_busy_ncu": load_profile_traffic(
                          key="fp64_pipe_busy_frac"),
+                     "fp64_pipe_busy_source": "the same committed ncu capture",
                      "avg_launch_us": 1e3 * ms.value / max(nl.value, 1),
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (measured)"
                      if peak else None},
@@ -285,28 +323,42 @@ def run_ours(a):
             gms, gby = _ct.c_double(0), _ct.c_double(0)
             L.ig_mixed_time_gs(sess._h, 1, 20, _ct.byref(gms), _ct.byref(gby))
             gs_gbs = gby.value / (gms.value * 1e-3) / 1e9
-            line["mixed"] = {
+            phi_m = np.array(phi_m[0])
+        tight = fp64_tight(fixed, val, 2.0)
+        line["mixed"] = {
                 "value": a.steps / el_m, "unit": "solves/s",
                 "path": "MixedSession.solve_values, pinned host buffers in and out",
                 "accuracy_of_span": 1e-9,
                 "refinement_steps": sess.last_steps,
                 "over_fp64_e2e": (a.steps / el_m) / (a.steps / el_e2e),
-                "max_abs_diff_vs_fp64_cascadic_of_span":
-                    float(np.abs(phi_m[0] - phi64).max()) / 2.0,
+                "max_abs_diff_vs_fp64_tight_of_span":
+                    float(np.abs(phi_m - tight).max()) / 2.0,
+                "fp64_tight": "drop-in V-cycle (solve3d_vmg) to a cycle "
+                              "delta of 1e-13 of the span",
+                "fp64_cascadic_diff_vs_fp64_tight_of_span":
+                    float(np.abs(phi64 - tight).max()) / 2.0,
                 "roofline": {"bound": "hbm", "kernel": "k_gs4 (FP32 split "
                              "red-black Gauss-Seidel, 13 B per updated node)",
                              "achieved": gs_gbs, "peak": peak, "unit": "GB/s",
                              "frac": gs_gbs / peak if peak else None,
                              "avg_launch_us": 1e3 * gms.value}}
+    if rank == 0 and ws == 1:
+        # the ring-stack batch (8 unit bases of a 193x193x385 deck): mixed
+        # precision against the FP64 drop-in basis door on the same box
+        line["rings"] = rings_measure(a)
     if rank == 0 and ws == 1 and not a.no_cpu:
-        g, pairs, secs, thr = cpu_sample(fixed, seconds=a.cpu_seconds)
+        secs, c_fine, c_rr, c_tot, c_lups, thr = cpu_full_solve(fixed, val)
         line["cpu_baseline"] = {
-            "value": g * 1e9 / lups, "unit": "solves/s", "cores": thr,
-            "kind": "port", "glup_s": g,
-            "sample": f"{pairs} red-black pairs of the reference sweep "
-                      f"(oracle C restatement, theta read as ones) on the "
-                      f"257^3 fine grid in {secs:.1f} s; solves/s = GLUP/s / "
-                      f"LUPs per solve ({lups:.4g})"}
+            "value": 1.0 / secs, "unit": "solves/s", "cores": thr,
+            "kind": "port", "glup_s": c_lups / secs / 1e9,
+            "sample": f"one complete solve of the workload by the oracle's "
+                      f"C restatement of the reference's sweep and residual "
+                      f"(theta read as ones), {secs:.1f} s; {c_fine} fine "
+                      f"pairs, {c_tot} on all levels",
+            "same_iterates_as_gpu": bool(c_fine == fine_pairs
+                                         and c_tot == total_pairs
+                                         and c_rr == relres),
+            "lups_per_solve": c_lups}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if ws > 1:
@@ -314,13 +366,13 @@ def run_ours(a):
         tdist.destroy_process_group()
 
 
-# LUPs of one solve of this workload (sum over levels of nodes x pairs); the
-# iterates are identical on every implementation (the GPU sweeps return the
-# reference's bits), so the count is a property of the workload.
-LUPS_PER_SOLVE = 26187534900   # 1500 fine pairs + 600 coarse-level pairs
-
-
 def run_reference(a):
+    """The reference's CPU path on the machine's host cores: the oracle's
+    restatement of the reference's sweep, residual, coarsening and
+    prolongation (C, OpenMP over all host threads; numba, which the
+    reference uses, is not installed on the GPU machine), each timed step one
+    complete solve of the workload; the warm-up steps run a few fine-grid
+    sweep pairs (page-in and thread start-up)."""
     ws, rank, _ = dist()
     if rank != 0:
         return
@@ -328,32 +380,33 @@ def run_reference(a):
     g.build_oracle()
     from oracle import port
     fixed, val = quadrupole()
-    lups = LUPS_PER_SOLVE
-    if lups is None:
-        print(json.dumps({"impl": "reference", "unavailable":
-                          "LUPs per solve of the workload not recorded yet"}))
-        return
-    per_step = max(2.0, a.cpu_seconds / 2)
-    vals = []
     port.set_threads(os.cpu_count() or 1)
-    for s in range(a.warmup + a.steps):
-        gl, pairs, secs, thr = cpu_sample(fixed, seconds=per_step)
-        if s >= a.warmup:
-            vals.append(gl)
-    g_mean = float(np.mean(vals))
-    v = g_mean * 1e9 / lups
+    for _ in range(a.warmup):
+        cpu_sample(fixed, seconds=0.5)
+    times = []
+    res = None
+    for _ in range(a.steps):
+        secs, fine, rr, tot, lups, thr = cpu_full_solve(fixed, val)
+        times.append(secs)
+        res = (fine, rr, tot, lups)
+    el = float(sum(times))
+    v = a.steps / el
+    fine, rr, tot, lups = res
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s",
         "n_gpus": ws, "steps": a.steps, "warmup": a.warmup,
-        "higher_is_better": True, "scaling": "weak", "dtype": "f64",
-        "config": {"workload": WORKLOAD, "grid": [N_SIDE] * 3},
-        "glup_s": g_mean,
+        "ms_per_step": 1e3 * el / a.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded geometry of the named workload)",
+        "config": workload_config(ws),
+        "glup_s": lups * a.steps / el / 1e9, "lups_per_solve": lups,
+        "fine_pairs": fine, "total_pairs": tot, "fine_relres": rr,
         "cpu_baseline": {"value": v, "unit": "solves/s", "cores": thr,
                          "kind": "port",
-                         "sample": f"each step: red-black pairs of the "
-                                   f"reference sweep (oracle C restatement) "
-                                   f"on the 257^3 fine grid for ~{per_step:.0f}"
-                                   f" s; solves/s = GLUP/s / {lups:.4g} LUPs"},
+                         "sample": f"each step one complete solve by the "
+                                   f"oracle's C restatement of the reference "
+                                   f"(theta read as ones), "
+                                   f"{1e3 * el / a.steps:.0f} ms per solve"},
         "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0}}), flush=True)
 
@@ -368,11 +421,15 @@ def _mixed_launches(L):
     return int(L.ig_mixed_launch_count())
 
 
-def run_rings(a):
-    """Batched ring-stack bases: the 8 unit bases of a seeded ring stack
-    (193x193x385) in one batch, mixed precision to 1e-9 of the span, against
-    the FP64 drop-in (the reference's V-cycle basis door at tol = 1e-9 x
-    span, bit-identical to the reference)."""
+def rings_measure(a, with_clocks=True):
+    """Batched ring-stack bases (BASELINE config 3): the 8 unit bases of a
+    seeded ring stack (193x193x385, grounded box) in one batch, mixed
+    precision to 1e-9 of the span, against the FP64 drop-in basis door (the
+    reference's V-cycle at tol = 1e-9 x span, bit-identical to the
+    reference) on the same bases.  Accuracy: two bases against the FP64
+    drop-in V-cycle run to a cycle delta of 1e-13 of the span, and every
+    basis against the basis door's result.  Returns the measurement dict."""
+    import contextlib
     import ctypes
     import torch
     from ion_gym_gb300 import _lib
@@ -389,30 +446,31 @@ def run_rings(a):
     for m in masks.values():
         metal |= m
     V, ACC = 1e4, 1e-9
-    sess = MixedSession(metal, len(rings))
+    nb = len(rings)
+    sess = MixedSession(metal, nb)
     # inputs resident in HBM: the stacked basis masks and the output
     stack = torch.from_numpy(
         np.stack([masks[i] for i in rings]).view(np.uint8)).cuda()
     out = torch.empty(stack.shape, dtype=torch.float64, device="cuda")
-    for _ in range(a.warmup):
+    for _ in range(max(a.warmup, 1)):
         sess.solve_bases(stack, V, ACC, out=out)
-    clocks = Clocks(0)
+    clocks = Clocks(0) if with_clocks else None
     launches0 = L.ig_launch_count() + _mixed_launches(L)
     torch.cuda.synchronize()
-    clocks.start()
+    if clocks:
+        clocks.start()
     t0 = time.perf_counter()
     for _ in range(a.steps):
         sess.solve_bases(stack, V, ACC, out=out)
     torch.cuda.synchronize()
     el = time.perf_counter() - t0
-    ck = clocks.stop()
+    ck = clocks.stop() if clocks else None
     launches = L.ig_launch_count() + _mixed_launches(L) - launches0
     phi = out.cpu().numpy()
     steps_per_solve = sess.last_steps
     ms = ctypes.c_double(0)
     by = ctypes.c_double(0)
-    L.ig_mixed_time_gs(sess._h, len(rings), 20, ctypes.byref(ms),
-                       ctypes.byref(by))
+    L.ig_mixed_time_gs(sess._h, nb, 20, ctypes.byref(ms), ctypes.byref(by))
     achieved = by.value / (ms.value * 1e-3) / 1e9
     # e2e through the public API: the session's solve from pinned host masks
     # to pinned host potentials (upload and download inside the timed region)
@@ -424,40 +482,55 @@ def run_rings(a):
     for _ in range(a.steps):
         sess.solve_bases(masks_h, V, ACC, out=out_h)
     el_e2e = time.perf_counter() - t1
+    sess.close()
     # the FP64 drop-in on the same bases
     tf = time.perf_counter()
-    import contextlib
     with contextlib.redirect_stdout(sys.stderr):    # the door's progress lines
         fp = MG.solve_bases_mg(masks, v_basis=V, tol=ACC * V, only=set(rings))
     el_fp = time.perf_counter() - tf
-    err = max(float(np.abs(phi[b] - fp[i]).max()) / V
-              for b, i in enumerate(rings))
+    err_door = max(float(np.abs(phi[b] - fp[i]).max()) / V
+                   for b, i in enumerate(rings))
+    del fp
+    tight = {}
+    for b in (0, nb // 2):
+        ref = fp64_tight(metal, np.where(masks[rings[b]], V, 0.0), V)
+        tight[rings[b]] = float(np.abs(phi[b] - ref).max()) / V
     n = metal.size
     peak = _peak()
-    line = {
-        "metric": METRIC, "value": len(rings) * a.steps / el,
-        "unit": "solves/s", "n_gpus": 1, "steps": a.steps,
+    mixed_v = nb * a.steps / el
+    res = {
+        "value": mixed_v, "unit": "solves/s", "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": 1e3 * el / a.steps,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32 sweeps + f64 refinement",
         "data": "synthetic (seeded ring stack)",
         "config": {"workload": "ring_stack_193x193x385_8_bases_mixed",
-                   "grid": list(box.shape), "bases": len(rings),
+                   "grid": list(box.shape), "bases": nb,
                    "accuracy_of_span": ACC, "refinement_steps": steps_per_solve,
-                   "l2": "inputs larger than L2"},
-        "fp64_dropin": {"value": len(rings) / el_fp, "unit": "solves/s",
-                        "method": "reference V-cycle basis door, tol 1e-5 V"},
-        "mixed_over_fp64": (len(rings) * a.steps / el) / (len(rings) / el_fp),
-        "max_abs_diff_vs_fp64_of_span": err,
-        "e2e": {"value": len(rings) * a.steps / el_e2e, "unit": "solves/s",
-                "h2d_bytes_per_step": n * len(rings),
-                "d2h_bytes_per_step": n * 8 * len(rings)},
+                   "l2": "inputs larger than L2 (14.3 M nodes x 8 bases)"},
+        "fp64_dropin": {"value": nb / el_fp, "unit": "solves/s",
+                        "method": "the reference's V-cycle basis door "
+                                  "(bit-identical), tol 1e-5 V = 1e-9 of "
+                                  "the span, 8 bases"},
+        "mixed_over_fp64": mixed_v / (nb / el_fp),
+        "max_abs_diff_vs_fp64_tight_of_span": max(tight.values()),
+        "diff_vs_fp64_tight_by_basis": {str(k): v for k, v in tight.items()},
+        "fp64_tight": "drop-in V-cycle (solve3d_vmg) to a cycle delta of "
+                      "1e-13 of the span",
+        "max_abs_diff_vs_fp64_door_of_span": err_door,
+        "e2e": {"value": nb * a.steps / el_e2e, "unit": "solves/s",
+                "h2d_bytes_per_step": n * nb,
+                "d2h_bytes_per_step": n * 8 * nb},
+        "e2e_over_fp64": (nb * a.steps / el_e2e) / (nb / el_fp),
         "gpu_launches": int(launches),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s",
                      "frac": achieved / peak if peak else None,
                      "traffic": load_profile_traffic("k_gs4_ring_stack.md"),
-                     "kernel": "k_gs (FP32 red-black split Gauss-Seidel)",
+                     "traffic_source": "ncu dram__bytes per launch from the "
+                     "committed capture profiles/k_gs4_ring_stack.md (not "
+                     "measured in this run)",
+                     "kernel": "k_gs4 (FP32 red-black split Gauss-Seidel, "
+                               "13 B per updated node)",
                      "avg_launch_us": 1e3 * ms.value},
         "clocks": ck,
     }
@@ -466,13 +539,23 @@ def run_rings(a):
         t = time.perf_counter()
         port.solve_bases_mg(masks, v_basis=V, tol=ACC * V, only={rings[0]})
         tc = time.perf_counter() - t
-        line["cpu_baseline"] = {
+        res["cpu_baseline"] = {
             "value": 1.0 / tc, "unit": "solves/s", "cores": port.num_threads(),
             "kind": "port",
             "sample": f"one basis (ring {rings[0]}) by the reference V-cycle "
                       f"basis door restated in oracle/ (C kernels, all host "
                       f"threads), {tc:.1f} s"}
-    sess.close()
+    return res
+
+
+def run_rings(a):
+    """The ring-stack batch as its own JSON line."""
+    r = rings_measure(a)
+    line = {"metric": METRIC, "value": r["value"], "unit": r["unit"],
+            "n_gpus": 1, "steps": r["steps"], "warmup": r["warmup"],
+            "ms_per_step": r["ms_per_step"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None}
+    line.update({k: v for k, v in r.items() if k not in line})
     print(json.dumps(line), flush=True)
 
 

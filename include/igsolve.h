@@ -223,10 +223,11 @@ int ig_mixed_check_fused(void *handle, int n_problems,
  * library holds until exit.  A grid whose coarse levels (about 2.4 bytes per
  * fine node) do not fit is refused with IG_BAD_ARG.  All calls share that
  * array and it keeps the last call's contents: calls that overlap on the GPU
- * race, so serialise them.  The first call on a device resolves the array's
- * device address (make it before any stream capture).  stream: the caller's
- * cudaStream_t (NULL = legacy default stream).  Same results, bit for bit,
- * as ig_cascadic_relres. */
+ * race, so serialise them.  Every call looks up the array's address on the
+ * current device (no allocation), so a device reset between calls is safe.
+ * The solve synchronises `stream` at every residual check.  stream: the
+ * caller's cudaStream_t (NULL = legacy default stream).  Same results, bit
+ * for bit, as ig_cascadic_relres. */
 #define IG_NOALLOC_SCRATCH_BYTES (48u * 1024u * 1024u)
 int ig_cascadic_relres_noalloc(const uint8_t *fixed, const double *val,
                                long nx, long ny, long nz, double rel_tol,

@@ -22,7 +22,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC",
 # per-file extra flags: the exact FP64 kernels forbid FMA contraction on top
 # of their explicit round-to-nearest intrinsics
 EXTRA = {"ig_f64.cu": ["--fmad=false"]}
-SOURCES = ["ig_f64.cu", "ig_f32.cu", "ig_solvers.cu", "ig_mixed.cu",
+SOURCES = ["ig_f64.cu", "ig_solvers.cu", "ig_mixed.cu",
            "ig_noalloc.cu", "ig_geometry.cu", "ig_field.cu"]
 
 

@@ -17,15 +17,16 @@
 // streams) race on it; serialise them.  The reduction slot is cleared before
 // every use; every coarse-level array is fully written before it is read.
 //
-// Set-up: the first call on a device resolves the device address of
-// g_noalloc_scratch with cudaGetSymbolAddress while that device is current
-// (host code cannot use the symbol itself: on the host it names a stand-in,
-// not device memory), and caches it per device.  Make that first call before
-// any stream capture.
+// Set-up: every call resolves the device address of g_noalloc_scratch with
+// cudaGetSymbolAddress on the calling thread's current device (host code
+// cannot use the symbol itself: on the host it names a stand-in, not device
+// memory).  The lookup allocates nothing, and resolving it per call keeps the
+// address right after a device reset or a new primary context, where the
+// module is loaded again and the array can move.  The solve synchronises the
+// stream at every residual check (the stop decision is taken on the host).
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
-#include <mutex>
 #include <string>
 
 #include "ig_common.cuh"
@@ -37,10 +38,6 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[IG_NOALLOC_SCRA
 
 namespace ig {
 namespace {
-
-constexpr int kMaxDevices = 64;
-std::mutex g_setup_mu;
-unsigned char* g_scratch_addr[kMaxDevices] = {nullptr};
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
@@ -124,19 +121,10 @@ extern "C" int ig_cascadic_relres_noalloc(
                     " bytes of scratch; the static scratch holds " +
                     std::to_string((size_t)IG_NOALLOC_SCRATCH_BYTES) +
                     " bytes (use ig_cascadic_relres for larger grids)");
-  int dev = 0;
-  NA_CK(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kMaxDevices) return fail(IG_BAD_ARG, "device index out of range");
-  unsigned char* base = nullptr;
-  {
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_addr[dev]) {
-      void* p = nullptr;
-      NA_CK(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-      g_scratch_addr[dev] = static_cast<unsigned char*>(p);
-    }
-    base = g_scratch_addr[dev];
-  }
+  // the array's address on the current device (see the file header)
+  void* sym = nullptr;
+  NA_CK(cudaGetSymbolAddress(&sym, g_noalloc_scratch));
+  unsigned char* base = static_cast<unsigned char*>(sym);
   cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
 
   // carve the hierarchy: level 0 is the caller's arrays, phi iterates in
@@ -204,8 +192,8 @@ extern "C" int ig_cascadic_relres_noalloc(
       if (rr < ltol || pairs >= max_sweeps) break;
       const int chunk = (int)std::min<long>(check_every, max_sweeps - pairs);
       for (int q = 0; q < chunk; q++) {
-        launch_sweep(s, M.phi, M.fixed, nullptr, kPlain, M.d, om, 0, red, nullptr, 0);
-        launch_sweep(s, M.phi, M.fixed, nullptr, kPlain, M.d, om, 1, red, nullptr, 0);
+        launch_sweep(s, M.phi, M.fixed, nullptr, kPlain, M.d, om, 0, nullptr, nullptr, 0);
+        launch_sweep(s, M.phi, M.fixed, nullptr, kPlain, M.d, om, 1, nullptr, nullptr, 0);
       }
       NA_CK(cudaGetLastError());
       pairs += chunk;

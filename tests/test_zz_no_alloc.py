@@ -30,7 +30,7 @@ def test_noalloc_matches_allocating_entry_point_twice():
     import torch
     from ion_gym_gb300 import _lib
     from ion_gym_gb300.physics import multigrid3d as MG
-    from ion_gym_gb300.workloads import quadrupole
+    from ion_gym_gb300.workloads import quadrupole, random_deck
     torch.cuda.set_device(0)
     L = _lib.lib()
     n = 97
@@ -39,14 +39,30 @@ def test_noalloc_matches_allocating_entry_point_twice():
     vd = torch.from_numpy(val).cuda()
     ref, ref_sw, ref_rr, ref_tot = MG.solve3d_cascadic_relres(
         fx, vd, 1e-10, 1.85, 4, 9, 20)
+    # a second deck of another shape and other Dirichlet values, solved
+    # between the two compared calls: it overwrites the shared scratch with
+    # coarse levels of other sizes and values, so the last call shows that
+    # every coarse array is written before it is read
+    f2, v2 = random_deck(77, 81, 6)
+    f2 = np.ascontiguousarray(f2[:, :65, :73])
+    v2 = np.ascontiguousarray(v2[:, :65, :73])
+    f2[:, -1] = True
+    f2[:, :, -1] = True
+    v2[:, -1] = 0.0
+    v2[:, :, -1] = 0.0
+    fx2 = torch.from_numpy(f2.view(np.uint8)).cuda()
+    vd2 = torch.from_numpy(v2).cuda()
+    ref2, ref2_sw, ref2_rr, ref2_tot = MG.solve3d_cascadic_relres(
+        fx2, vd2, 1e-10, 1.85, 4, 9, 20)
     omega = np.full(4, 1.85)
     outs = [torch.empty_like(vd) for _ in range(2)]
+    out2 = torch.empty_like(vd2)
     stream = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     torch.cuda.synchronize()
-    # first call resolves the scratch address; the second must not touch
-    # the allocator at all
     first = _call(L, fx, vd, outs[0], (n, n, n), stream, omega)
+    other = _call(L, fx2, vd2, out2, f2.shape, stream, omega)
     torch.cuda.synchronize()
+    # the last call must not touch the allocator at all
     free_before = torch.cuda.mem_get_info()[0]
     second = _call(L, fx, vd, outs[1], (n, n, n), stream, omega)
     torch.cuda.synchronize()
@@ -54,9 +70,12 @@ def test_noalloc_matches_allocating_entry_point_twice():
     for st, sw, rr, tot, nl in (first, second):
         assert st == _lib.IG_OK, _lib.last_error()
         assert (sw, rr, tot, nl) == (ref_sw, ref_rr, ref_tot, 4)
+    assert other[0] == _lib.IG_OK, _lib.last_error()
+    assert other[1:4] == (ref2_sw, ref2_rr, ref2_tot)
+    # FP64 path: the tolerance of these tests is bit equality
     for o in outs:
-        # FP64 path: the tolerance of these tests is bit equality
         assert torch.equal(o.view(torch.int64), ref.view(torch.int64))
+    assert torch.equal(out2.view(torch.int64), ref2.view(torch.int64))
     assert free_after == free_before
 
 
