@@ -19,11 +19,11 @@ place; the first writer wins and a loser's copy is removed.
 import hashlib
 import json
 import os
-import shutil
-import tempfile
 from pathlib import Path
 
 import numpy as np
+
+from ion_gym_gb300.io.publish import staged, write_json
 
 CACHE_VERSION = 2
 
@@ -84,14 +84,9 @@ def store(spec, arrays, root=None):
     root = _root(root)
     key = spec_key(spec)
     dest = os.path.join(root, key)
-    if os.path.exists(os.path.join(dest, "meta.json")):
-        if _complete(dest):
-            return key
-        shutil.rmtree(dest, ignore_errors=True)
-    os.makedirs(root, exist_ok=True)
-    tmp = tempfile.mkdtemp(prefix=f".{key}.", dir=root)
-    published = False
-    try:
+    if _complete(dest):
+        return key
+    with staged(dest, folder=True, keep_if=_complete) as tmp:
         manifest = {}
         for name, a in arrays.items():
             a = np.ascontiguousarray(a)
@@ -100,19 +95,9 @@ def store(spec, arrays, root=None):
                               "sha_head": sha_head(a)}
         meta = {"key": key, "version": CACHE_VERSION, "spec": spec,
                 "arrays": manifest}
+        # meta.json is the completeness marker: written last
         with open(os.path.join(tmp, "meta.json"), "w", encoding="utf-8") as f:
             json.dump(meta, f, indent=1)
-            f.flush()
-            os.fsync(f.fileno())
-        try:
-            os.replace(tmp, dest)
-            published = True
-        except OSError:
-            if not os.path.exists(os.path.join(dest, "meta.json")):
-                raise
-    finally:
-        if not published and os.path.isdir(tmp):
-            shutil.rmtree(tmp, ignore_errors=True)
     return key
 
 
@@ -200,92 +185,118 @@ def load_bases(spec_or_key, root=None):
     return bases, {i: (lab == i) for i in bases}
 
 
-def annotate(spec_or_key, name, label=None, root=None, spec_json=None):
-    """Record which named spec produced or resolved an entry in its
-    provenance.json sidecar (fa_cache.py:219-272): a list of {name, label,
-    when[, spec_json]} records; a repeated (name, label) refreshes its time
-    (and spec_json).  Descriptive only: an unreadable sidecar is rebuilt
-    and a write failure is reported, never raised."""
-    import time
-    key = (spec_or_key if isinstance(spec_or_key, str) else spec_key(spec_or_key))
-    name = (name or "").strip()
-    if not name:
-        return
-    dest = os.path.join(os.path.expanduser(_root(root)), key)
-    if not os.path.isdir(dest):
-        return
-    ppath = os.path.join(dest, "provenance.json")
-    recs = []
-    if os.path.exists(ppath):
-        try:
-            with open(ppath, encoding="utf-8") as f:
-                recs = json.load(f)
-            if not isinstance(recs, list):
-                raise ValueError(f"expected a list, got {type(recs).__name__}")
-        except (OSError, ValueError) as e:
-            print(f"fa_cache: provenance sidecar unreadable for {key} "
-                  f"({e}) — rebuilding it (descriptive data only).")
-            recs = []
-    now = time.strftime("%Y-%m-%d %H:%M")
-    for r in recs:
-        if r.get("name") == name and r.get("label") == label:
-            r["when"] = now
-            if spec_json is not None:
-                r["spec_json"] = spec_json
-            break
-    else:
-        rec = dict(name=name, label=label, when=now)
-        if spec_json is not None:
-            rec["spec_json"] = spec_json
-        recs.append(rec)
+PROVENANCE = "provenance.json"
+
+
+def _read_json(path):
+    """(object, None) of a JSON file, (None, reason) when it is unreadable,
+    (None, None) when it does not exist."""
     try:
-        fd, tmp = tempfile.mkstemp(dir=dest, prefix=".prov.")
-        with os.fdopen(fd, "w") as f:
-            json.dump(recs, f, indent=1)
-        os.replace(tmp, ppath)
+        with open(path, encoding="utf-8") as f:
+            return json.load(f), None
+    except FileNotFoundError:
+        return None, None
+    except (OSError, ValueError) as e:
+        return None, f"{type(e).__name__}: {e}"
+
+
+def _records(entry_dir):
+    """(provenance records, problem) of an entry: [] and a reason when the
+    sidecar is unreadable or not a list of records."""
+    recs, why = _read_json(os.path.join(entry_dir, PROVENANCE))
+    if why is None and recs is not None and not isinstance(recs, list):
+        why = f"expected a list of records, found {type(recs).__name__}"
+    if why is not None or recs is None:
+        return [], why
+    return [r for r in recs if isinstance(r, dict)], None
+
+
+def latest_spec_json(records):
+    """The producing spec of the newest record that carries one, or None."""
+    for r in reversed(records):
+        if r.get("spec_json"):
+            return r["spec_json"]
+    return None
+
+
+def annotate(spec_or_key, name, label=None, root=None, spec_json=None):
+    """Record in the entry's provenance.json sidecar that the spec `name`
+    (with `label`) produced or resolved it (fa_cache.py:219-272): one
+    {name, label, when[, spec_json]} record per (name, label); naming the
+    same pair again refreshes its time and spec_json.  The sidecar is
+    descriptive only: an unreadable one is started afresh, and a failed
+    write is reported on stdout, never raised.  Missing entries and empty
+    names are ignored."""
+    import time
+    key = spec_or_key if isinstance(spec_or_key, str) else spec_key(spec_or_key)
+    name = (name or "").strip()
+    entry = os.path.join(os.path.expanduser(_root(root)), key)
+    if not name or not os.path.isdir(entry):
+        return
+    recs, why = _records(entry)
+    if why is not None:
+        print(f"fa_cache: entry {key}: starting a new provenance record "
+              f"list, the old one could not be read ({why})")
+    stamp = {"when": time.strftime("%Y-%m-%d %H:%M")}
+    if spec_json is not None:
+        stamp["spec_json"] = spec_json
+    mine = [r for r in recs if (r.get("name"), r.get("label")) == (name, label)]
+    if mine:
+        mine[0].update(stamp)
+    else:
+        recs.append({"name": name, "label": label, **stamp})
+    try:
+        write_json(os.path.join(entry, PROVENANCE), recs)
     except OSError as e:
-        print(f"fa_cache: could not write provenance for {key} ({e})")
+        print(f"fa_cache: entry {key}: provenance not written ({e})")
+
+
+def _describe(entry_dir):
+    """One inventory row of an entry folder; never raises."""
+    files = []
+    for dp, _, fn in os.walk(entry_dir):
+        files += [os.path.join(dp, f) for f in fn]
+    size = unsized = 0
+    for f in files:
+        try:
+            size += os.path.getsize(f)
+        except OSError:
+            unsized += 1
+    row = {"key": os.path.basename(entry_dir), "bytes": size,
+           "unsized_files": unsized,
+           "arrays": sum(f.endswith(".npy") for f in files),
+           "mtime": os.path.getmtime(entry_dir), "spec_name": None,
+           "shape": None, "produced_by": [], "descriptor": None,
+           "has_spec_json": False, "problems": []}
+    recs, why = _records(entry_dir)
+    if why is not None:
+        row["problems"].append(f"{PROVENANCE} unreadable ({why})")
+    row["produced_by"] = [r["name"] for r in recs if r.get("name")]
+    labels = [r["label"] for r in recs if r.get("label")]
+    row["descriptor"] = labels[-1] if labels else None
+    row["has_spec_json"] = latest_spec_json(recs) is not None
+    meta, why = _read_json(os.path.join(entry_dir, "meta.json"))
+    if why is not None:
+        row["problems"].append(f"meta.json unreadable ({why})")
+    elif isinstance(meta, dict):
+        spec = meta.get("spec")
+        if isinstance(spec, dict):
+            row["spec_name"] = spec.get("name")
+        shapes = [a.get("shape") for a in (meta.get("arrays") or {}).values()
+                  if isinstance(a, dict)]
+        row["shape"] = shapes[0] if shapes else None
+    return row
 
 
 def entries(root=None):
-    """[{key, arrays, spec_name, shape, produced_by, has_spec_json}] of the
-    complete-or-not entries under root (fa_cache.py:275-330, the fields a
-    field export needs)."""
+    """Inventory of the cache (fa_cache.py:275-330): one row per entry
+    folder, in key order -- key, bytes on disk (unsized_files counts files
+    whose size could not be read), .npy count, mtime, the stored spec's
+    name, the first array's shape, the names that produced it, its latest
+    label, whether a producing spec JSON is recorded, and the problems met
+    reading it."""
     root = os.path.expanduser(_root(root))
-    out = []
     if not os.path.isdir(root):
-        return out
-    for name in sorted(os.listdir(root)):
-        p = os.path.join(root, name)
-        if not os.path.isdir(p) or name.startswith("."):
-            continue
-        rec = dict(key=name, arrays=sum(f.endswith(".npy") for f in os.listdir(p)),
-                   spec_name=None, shape=None, produced_by=[], has_spec_json=False,
-                   problems=[])
-        ppath = os.path.join(p, "provenance.json")
-        if os.path.exists(ppath):
-            try:
-                with open(ppath, encoding="utf-8") as f:
-                    precs = json.load(f)
-                if isinstance(precs, list):
-                    rec["produced_by"] = [r.get("name") for r in precs
-                                          if isinstance(r, dict) and r.get("name")]
-                    rec["has_spec_json"] = any(isinstance(r, dict) and r.get("spec_json")
-                                               for r in precs)
-            except (OSError, ValueError) as e:
-                rec["problems"].append(
-                    f"provenance.json unreadable ({type(e).__name__}: {e})")
-        mp = os.path.join(p, "meta.json")
-        if os.path.exists(mp):
-            try:
-                with open(mp, encoding="utf-8") as f:
-                    meta = json.load(f)
-                spec = meta.get("spec", {}) or {}
-                rec["spec_name"] = spec.get("name") if isinstance(spec, dict) else None
-                arrs = meta.get("arrays", {}) or {}
-                if arrs:
-                    rec["shape"] = next(iter(arrs.values())).get("shape")
-            except (OSError, ValueError, KeyError, AttributeError) as e:
-                rec["problems"].append(f"meta.json unreadable ({type(e).__name__}: {e})")
-        out.append(rec)
-    return out
+        return []
+    return [_describe(os.path.join(root, n)) for n in sorted(os.listdir(root))
+            if not n.startswith(".") and os.path.isdir(os.path.join(root, n))]

@@ -113,3 +113,46 @@ def test_refusals_and_labels(tmp_path):
     assert field_io.read_field_meta(npz)["spec_name"] == "ring deck"
     assert field_io.resolve_cache_entry({"geometry": MG.bundle_spec()[2]["geometry"]},
                                         root=root) == key
+
+
+def test_geometry_diff_paths_and_order():
+    a = {"mm_per_gu": 0.25, "electrodes": [{"name": "e1", "v": 1.0},
+                                           {"name": "e2", "v": 2.0}],
+         "grid": {"nx": 10, "ny": 12}, "only_a": 1}
+    b = {"mm_per_gu": 0.25, "electrodes": [{"name": "e1", "v": 1.5},
+                                           {"name": "e2", "v": 2.0, "w": 3}],
+         "grid": {"nx": 10, "ny": [12]}, "only_b": 2}
+    assert field_io.geometry_diff(a, b) == [
+        "electrodes.[0].v: 1.0 vs 1.5",
+        "electrodes.[1].w: <absent> vs present",
+        "grid.ny: 12 vs [12]",
+        "only_a: present vs <absent>",
+        "only_b: <absent> vs present"]
+    assert field_io.geometry_diff({"e": [1, 2]}, {"e": [1]}) == ["e: length 2 vs 1"]
+    assert field_io.geometry_diff(a, a) == []
+
+
+def test_inventory_and_provenance(tmp_path):
+    key, root = _entry(tmp_path)
+    fa_cache.annotate(key, "ring deck", label="first", root=root)    # refresh
+    fa_cache.annotate(key, "other deck", label=None, root=root)
+    fa_cache.annotate(key, "   ", root=root)                          # ignored
+    recs = json.load(open(os.path.join(root, key, "provenance.json")))
+    assert [(r["name"], r["label"]) for r in recs] == [("ring deck", "first"),
+                                                       ("other deck", None)]
+    assert "spec_json" in recs[0] and "spec_json" not in recs[1]
+    (row,) = fa_cache.entries(root=root)
+    assert row["key"] == key and row["arrays"] == 3 and row["problems"] == []
+    assert row["produced_by"] == ["ring deck", "other deck"]
+    assert row["descriptor"] == "first" and row["has_spec_json"]
+    assert row["spec_name"] == "ring deck" and row["bytes"] > 0
+    # an unreadable sidecar is reported by the inventory and started afresh
+    # by the next annotation
+    with open(os.path.join(root, key, "provenance.json"), "w") as f:
+        f.write("{not json")
+    (row,) = fa_cache.entries(root=root)
+    assert row["produced_by"] == [] and "unreadable" in row["problems"][0]
+    fa_cache.annotate(key, "again", root=root)
+    assert [r["name"] for r in json.load(
+        open(os.path.join(root, key, "provenance.json")))] == ["again"]
+    assert fa_cache.entries(root=str(tmp_path / "none")) == []
