@@ -150,14 +150,17 @@ STL3D_SOLVE_TOL = 1e-4  # physics/build_stl3d.py:40
 
 
 def solve_stl3d_bases(masks, mirror_axes=(False, False, False),
-                      verbose=False):
+                      verbose=False, precision=None):
     """physics/build_stl3d._solve_stl3d_bases (build_stl3d.py:835-849): the
-    V-cycle basis door at V_BASIS and STL3D_SOLVE_TOL, returned as float32
-    unit bases."""
+    basis door at V_BASIS and STL3D_SOLVE_TOL, returned as float32 unit
+    bases.  precision (not in the reference signature): None / "fp64" runs
+    the reference's V-cycle (its bits), "mixed" the batched mixed-precision
+    session to the same tolerance; solve_code.solve_code_key(precision)
+    keys the cache entry on the choice."""
     from ion_gym_gb300.physics.multigrid3d import solve_bases_mg
     bases = solve_bases_mg(masks, mirror=mirror_axes, v_basis=V_BASIS,
                            tol=STL3D_SOLVE_TOL, stencil="ghost_linear",
-                           verbose=verbose)
+                           verbose=verbose, precision=precision)
     return {i: (b / V_BASIS).astype(np.float32) for i, b in bases.items()}
 
 

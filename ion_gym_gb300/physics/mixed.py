@@ -171,22 +171,51 @@ class MixedSession:
             pass
 
 
+def max_batch(shape, n_bases, budget_frac=0.8):
+    """How many bases of this grid one MixedSession can hold in the free
+    device memory (at least 1)."""
+    try:
+        free = int(_lib.lib().ig_device_free_bytes())
+    except Exception:
+        free = 0
+    if free <= 0:
+        return max(1, n_bases)
+    b = max(1, n_bases)
+    while b > 1 and session_bytes(shape, b) > budget_frac * free:
+        b = (b + 1) // 2
+    return b
+
+
 def solve_bases_mixed(masks, v_basis=1e4, accuracy=1e-9,
                       stencil="ghost_linear", only=None, max_steps=40,
-                      return_stats=False, **cycle):
-    """All bases in one batch.  Returns {index: phi}; with return_stats also
-    {"steps": refinement steps}.  cycle: overrides of CYCLE."""
+                      return_stats=False, batch=None, on_batch=None, **cycle):
+    """All bases of a deck by the mixed-precision session: {index: mask} ->
+    {index: phi float64 at v_basis}.  The bases run in batches of `batch`
+    (default: as many as free device memory holds, all of them when they
+    fit) on one resident session.  on_batch(done, total, indices), when
+    given, is called before each batch (and may raise to stop).  With
+    return_stats, also {"steps": the largest refinement-step count of any
+    batch, "batches": n}.  cycle: overrides of CYCLE."""
     metal = _union(masks)
     items = [(i, np.asarray(m, bool)) for i, m in sorted(masks.items())
              if only is None or i in only]
     if not items:
-        return ({}, {"steps": 0}) if return_stats else {}
-    with MixedSession(metal, len(items), stencil=stencil,
-                      **{**CYCLE, **cycle}) as s:
-        phi = s.solve_bases([m for _, m in items], v_basis, accuracy,
-                            max_steps)
-        steps = s.last_steps
-    out = {i: phi[b] for b, (i, _) in enumerate(items)}
+        return ({}, {"steps": 0, "batches": 0}) if return_stats else {}
+    B = int(batch) if batch else max_batch(metal.shape, len(items))
+    B = max(1, min(B, len(items)))
+    out = {}
+    steps = 0
+    nb = 0
+    with MixedSession(metal, B, stencil=stencil, **{**CYCLE, **cycle}) as s:
+        for q in range(0, len(items), B):
+            part = items[q:q + B]
+            if on_batch is not None:
+                on_batch(q, len(items), [i for i, _ in part])
+            phi = s.solve_bases([m for _, m in part], v_basis, accuracy,
+                                max_steps)
+            out.update({i: phi[b] for b, (i, _) in enumerate(part)})
+            steps = max(steps, s.last_steps)
+            nb += 1
     if return_stats:
-        return out, {"steps": steps}
+        return out, {"steps": steps, "batches": nb}
     return out

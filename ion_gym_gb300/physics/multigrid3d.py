@@ -271,18 +271,84 @@ def _basis_workers(n_bases, n_nodes):
     return w
 
 
+# How the basis door solves when its caller does not say: "fp64", the
+# reference's V-cycle with its bits, or "mixed", the batched FP32-multigrid /
+# FP64-refinement session (IG_BASIS_PRECISION overrides the default).
+PRECISIONS = ("fp64", "mixed")
+BASIS_PRECISION = os.environ.get("IG_BASIS_PRECISION", "fp64")
+
+
+def basis_precision(precision=None):
+    """The precision a basis solve runs in: `precision`, else the module's
+    BASIS_PRECISION; refuses anything but 'fp64' and 'mixed'."""
+    p = BASIS_PRECISION if precision is None else precision
+    if p not in PRECISIONS:
+        raise ValueError(f"unknown basis precision {p!r}; known precisions "
+                         f"are 'fp64' and 'mixed'")
+    return p
+
+
+def _solve_bases_mixed_door(masks, todo, v_basis, tol, stencil, verbose):
+    """The basis door's mixed-precision form: every requested basis in
+    batched mixed-precision sessions, each to tol volts (tol / |v_basis|
+    of the electrode span, in the max norm against the converged FP64
+    solution of the same discrete problem)."""
+    from ion_gym_gb300.physics.mixed import solve_bases_mixed
+    n = len(masks)
+    want = {i for _, i, _ in todo}
+
+    def progress(done, total, idx):
+        if _STOP.is_set():
+            raise SolveInterrupted(f"stopped after {done} of {n} electrodes")
+        print(f"  [{time.strftime('%H:%M:%S')}] solving electrodes "
+              f"{idx[0]}..{idx[-1]} ({done + len(idx)} of {total}) in one "
+              f"mixed-precision batch ...", flush=True)
+
+    if _STOP.is_set():
+        raise SolveInterrupted(f"stopped after 0 of {n} electrodes")
+    t0 = time.time()
+    out, st = solve_bases_mixed(masks, v_basis=v_basis,
+                                accuracy=float(tol) / abs(float(v_basis)),
+                                stencil=stencil, only=want, return_stats=True,
+                                on_batch=progress)
+    secs = time.time() - t0
+    print(f"  {len(out)} bases in {st['batches']} mixed-precision batch(es), "
+          f"{st['steps']} refinement steps ({secs:.1f}s)", flush=True)
+    shape = next(iter(masks.values())).shape
+    for _ in out:
+        _record_solve(int(np.prod(shape)), secs / max(len(out), 1))
+    return {i: out[i] for _, i, _ in todo}
+
+
 def solve_bases_mg(masks, scene=None, mirror=(False, False, False),
                    v_basis=1e4, tol=1e-6, verbose=False,
-                   stencil="ghost_linear", theta=None, only=None):
+                   stencil="ghost_linear", theta=None, only=None,
+                   precision=None):
     """The basis door (multigrid3d.py:233-291): for each electrode, in
     index order, the V-cycle on the metal union with that electrode at
     v_basis and the rest at 0.  Raises SolveInterrupted between bases after
     request_stop(), and refuses to return a basis whose delta is not below
     tol.  Up to BASIS_CONCURRENCY bases run at once (each on its own
     stream); progress lines, refusals and the returned dict follow the
-    electrode order exactly as a one-at-a-time loop gives them."""
+    electrode order exactly as a one-at-a-time loop gives them.
+
+    precision (not in the reference signature; default BASIS_PRECISION,
+    "fp64"): "mixed" solves the bases in batches by the mixed-precision
+    session instead, each to tol volts of the converged solution (max
+    norm); it takes theta None only (no scene, no theta)."""
     from concurrent.futures import ThreadPoolExecutor
+    prec = basis_precision(precision)
     metal = _union(masks)
+    if prec == "mixed":
+        if scene is not None or theta is not None:
+            raise ValueError("solve_bases_mg: precision='mixed' solves the "
+                             "plain stencil only (theta None); pass no scene "
+                             "or theta, or use precision='fp64'")
+        stencil_code(stencil)
+        todo = [(j, i, m) for j, (i, m) in enumerate(sorted(masks.items()), 1)
+                if only is None or i in only]
+        return _solve_bases_mixed_door(masks, todo, v_basis, tol, stencil,
+                                       verbose)
     th = theta
     if th is None and scene is not None:
         th = fractions_from_scene(scene, metal, mirror=mirror)

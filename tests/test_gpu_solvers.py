@@ -176,3 +176,64 @@ def test_shortley_weller_vcycle_matches_oracle(M):
     a = M.solve3d_vmg(fixed, val, tol=1e-5, stencil="sw")
     b = port.solve3d_vmg(fixed, val, tol=1e-5, stencil="sw")
     assert a[1:] == b[1:] and same_bits(a[0], b[0])
+
+
+def test_solve_stl3d_bases_golden_and_mixed(M, drivers_golden):
+    """build_stl3d._solve_stl3d_bases (build_stl3d.py:835-849): the basis
+    door at tol 1e-4 V, v_basis 1e4, as float32 unit bases -- the golden
+    deck's bases 1 and 2 are the reference's own (b / 1e4) rounded to
+    float32 bit for bit, basis 3 the oracle's; the mixed-precision form of
+    the same call lands within the tolerance of the two solves (1e-4 V of
+    1e4 V each) plus one float32 rounding."""
+    from ion_gym_gb300.io import fa_cache
+    (m,) = drivers_golden.cases("bases_mg")
+    masks = {1: m["m1"].astype(bool), 2: m["m2"].astype(bool),
+             3: m["m3"].astype(bool)}
+    got = fa_cache.solve_stl3d_bases(masks)
+    assert sorted(got) == [1, 2, 3]
+    for i in (1, 2):
+        want = (m[f"b{i}"] / 1e4).astype(np.float32)
+        assert got[i].dtype == np.float32
+        assert np.array_equal(got[i].view(np.uint32), want.view(np.uint32))
+    o3 = port.solve_bases_mg(masks, v_basis=1e4, tol=1e-4, only={3})[3]
+    assert np.array_equal(got[3].view(np.uint32),
+                          (o3 / 1e4).astype(np.float32).view(np.uint32))
+    mixed = fa_cache.solve_stl3d_bases(masks, precision="mixed")
+    for i in (1, 2, 3):
+        assert mixed[i].dtype == np.float32
+        assert np.abs(mixed[i].astype(np.float64) - got[i]).max() <= 2e-8 + 2.0 ** -23
+
+
+def test_basis_door_mixed_precision_batches(M):
+    """solve_bases_mg(precision='mixed'): the requested bases, in index
+    order, within 1e-9 of the span of the FP64 door's result at a tight
+    tolerance, the same with several small batches as with one, and the
+    stop flag honoured before the first batch."""
+    rng = np.random.default_rng(21)
+    shape = (37, 41, 33)
+    box = np.zeros(shape, bool)
+    box[0] = box[-1] = True
+    box[:, 0] = box[:, -1] = True
+    box[:, :, 0] = box[:, :, -1] = True
+    masks = {9: box}
+    i, j, k = np.ogrid[:37, :41, :33]
+    for e in (2, 3, 5, 7):
+        c = rng.uniform(8, 28, 3)
+        masks[e] = ((i - c[0]) ** 2 + (j - c[1]) ** 2 + (k - c[2]) ** 2
+                    <= rng.uniform(9, 25)) & ~box
+    ref = M.solve_bases_mg(masks, tol=1e-9, only={2, 5, 7})
+    got = M.solve_bases_mg(masks, tol=1e-5, only={2, 5, 7}, precision="mixed")
+    assert list(got) == [2, 5, 7]
+    for e in got:
+        assert np.abs(got[e] - ref[e]).max() <= 1e-9 * 1e4 + 1e-9 * 1e4
+    from ion_gym_gb300.physics.mixed import solve_bases_mixed
+    small = solve_bases_mixed(masks, v_basis=1e4, accuracy=1e-9,
+                              only={2, 5, 7}, batch=2)
+    for e in got:
+        assert np.abs(small[e] - got[e]).max() <= 2e-9 * 1e4
+    M.request_stop()
+    try:
+        with pytest.raises(M.SolveInterrupted, match="stopped after 0"):
+            M.solve_bases_mg(masks, tol=1e-5, precision="mixed")
+    finally:
+        M.clear_stop()
