@@ -143,9 +143,9 @@ int ig_cascadic_relres(const uint8_t *fixed, const double *val, long nx,
  * preconditioned by one FP32 red-black multigrid V-cycle (nu1/nu2
  * Gauss-Seidel pairs), refine the FP64 potential, whose residual is the
  * reference's fine operator with theta None (formed exactly); a basis is
- * done when the last refinement step d and the geometric tail estimate
- * d * rho / (1 - rho) (rho the observed step ratio) are both below `acc`
- * (absolute, volts).  Out: phi (n_bases x n float64), refinement steps, and
+ * done when the geometric tail d * rho / (1 - rho) of its last refinement
+ * step d is below `acc` (absolute, volts), rho being 3 x the larger of the
+ * last two observed step ratios.  Out: phi (n_bases x n float64), refinement steps, and
  * each basis's last step.  IG_NOT_CONVERGED after max_steps. */
 int ig_mixed_bases(const uint8_t *metal, const uint8_t *masks, int n_bases,
                    double v_basis, long nx, long ny, long nz, int stencil,

@@ -14,8 +14,9 @@
 //                  multigrid V-cycle (block-ANY coarse masks, 13-point
 //                  restriction of the colour-0 residual, trilinear
 //                  prolongation, red-black Gauss-Seidel, one-CTA bottom)
-//            phi64 += x32;  stop when the step and its geometric tail
-//                           estimate are below acc     (per problem)
+//            phi64 += x32;  stop when the geometric tail estimated from
+//                           the observed step contraction is below acc
+//                           (per problem)
 //   (method 0 replaces the CG by `vcycles` plain V-cycles per step)
 //
 // FP32 data live in a red-black split layout: colour c of row (i, j) holds
@@ -1777,14 +1778,20 @@ struct MixedResult {
 };
 
 // Refinement steps until every problem is within acc of its converged
-// potential.  The step contraction rho is estimated from successive applied
-// changes d_k / d_{k-1}; the remaining error after step k is then at most
-// about d_k * rho / (1 - rho) (a geometric tail).  A problem is done when
-// that bound and d_k itself are below acc.
+// potential.  With d_k the max |change| applied by step k and
+// rho_k = d_k / d_{k-1} its observed contraction, the error left after step k
+// is the sum of the later changes, d_{k+1} + d_{k+2} + ... (measured against
+// the converged FP64 solution on the benchmark decks: within a few percent
+// of d_{k+1}).  rho_{k+1} is estimated as kRhoSafety times the larger of the
+// last two observed ratios, and a problem is done when the geometric tail
+// d_k rho / (1 - rho) of that estimate is below acc (or when d_k is 0).  The
+// first step has no ratio and never stops a problem with a nonzero change.
+constexpr double kRhoSafety = 3.0;
+
 MixedResult run_mixed(Session& M, double acc, int max_steps) {
   if (M.method == 1) M.cg_init();
   std::vector<unsigned long long> h(M.B);
-  std::vector<double> prev(M.B, INFINITY);
+  std::vector<double> prev(M.B, INFINITY), prev_rho(M.B, 0.0);
   MixedResult res{IG_NOT_CONVERGED, 0, std::vector<double>(M.B, 0.0)};
   for (int it = 0; it < max_steps; it++) {
     M.step();
@@ -1795,11 +1802,12 @@ MixedResult run_mixed(Session& M, double acc, int max_steps) {
     for (int b = 0; b < M.B; b++) {
       const double d = bits_to_double(h[b]);
       res.dmax[b] = d;
-      double rho = std::isfinite(prev[b]) && prev[b] > 0 ? d / prev[b] : 1.0;
-      rho = std::min(std::max(rho, 0.05), 0.95);
+      const double r = std::isfinite(prev[b]) && prev[b] > 0 ? d / prev[b] : 1.0;
+      const double rho = std::min(kRhoSafety * std::max(r, prev_rho[b]), 0.95);
       const double tail = d * rho / (1.0 - rho);
-      if (!(d < acc && tail < acc) && !(d == 0.0)) all = false;
+      if (!(tail < acc) && !(d == 0.0)) all = false;
       prev[b] = d;
+      prev_rho[b] = r;
     }
     if (all) {
       res.status = IG_OK;

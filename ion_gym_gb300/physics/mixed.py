@@ -3,11 +3,12 @@ one batch, FP32 multigrid inside FP64 iterative refinement.
 
 Same inputs and outputs as multigrid3d.solve_bases_mg ({index: mask} ->
 {index: phi float64 at v_basis}) but a different stopping rule: each basis
-is refined until the applied FP64 change of a refinement step is below
-`accuracy` x the electrode span (v_basis), so the potential is within about
-that accuracy of the exact solution of the same discrete problem (the
-reference's fine operator: theta None, 7-point, even-reflection faces,
-Dirichlet metal).  The FP64 drop-in solves the same problem with the
+is refined until the error left after a refinement step, estimated from
+that step's applied FP64 change and the observed contraction of the
+changes, is below `accuracy` x the electrode span (v_basis), so the
+potential is within that accuracy of the exact solution of the same
+discrete problem (the reference's fine operator: theta None, 7-point,
+even-reflection faces, Dirichlet metal).  The FP64 drop-in solves the same problem with the
 reference's V-cycle and its cycle-delta rule; the two agree to the stated
 accuracy (tests/test_gpu_mixed.py).
 """
