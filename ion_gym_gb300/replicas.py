@@ -99,3 +99,58 @@ def solve_bases_sharded(masks, rank=None, size=None, **kwargs):
     if only is not None:
         mine &= set(only)
     return MG.solve_bases_mg(masks, only=mine, **kwargs)
+
+
+def solve_bases_mixed_sharded(masks, spec=None, root=None, rank=None,
+                              size=None, v_basis=1e4, accuracy=1e-9, **kwargs):
+    """The mixed-precision basis batch of one deck, sharded over the ranks:
+    each rank solves its round-robin share of the bases in its own batched
+    session (physics.mixed.solve_bases_mixed; `only` narrows the set) and
+    returns {index: phi float64 at v_basis} for that share.
+
+    With `spec`, the ranks' results also become one cache entry in the
+    reference's 3-D layout (build_stl3d.py:919-924: float32 unit bases
+    basis_<i> and the uint8 labels): each rank stages its unit bases as .npy
+    files in a folder beside the cache (the gather goes through the shared
+    disk of the node, not through the process group), and after a barrier
+    rank 0 stores the entry from them (fa_cache.store, published
+    atomically) and removes the staging folder.  Every rank returns
+    (its bases, the entry key) then."""
+    import numpy as np
+    from ion_gym_gb300.physics import mixed
+    from ion_gym_gb300.io import fa_cache
+    if rank is None or size is None:
+        size, rank, _ = world()
+    mine = set(shard(masks.keys(), rank, size))
+    only = kwargs.pop("only", None)
+    if only is not None:
+        mine &= set(only)
+    out = mixed.solve_bases_mixed(masks, v_basis=v_basis, accuracy=accuracy,
+                                  only=mine, **kwargs) if mine else {}
+    if spec is None:
+        return out
+    key = fa_cache.spec_key(spec)
+    base = os.path.expanduser(fa_cache._root(root))
+    stage = os.path.join(base, f".{key}.shards")
+    os.makedirs(stage, exist_ok=True)
+    for i, phi in out.items():
+        unit = (np.asarray(phi) / v_basis).astype(np.float32)
+        tmp = os.path.join(stage, f".basis_{i}.{rank}.npy")
+        np.save(tmp, unit)
+        os.replace(tmp, os.path.join(stage, f"basis_{i}.npy"))
+    barrier()
+    if rank == 0:
+        want = sorted(i for i in masks if only is None or i in only)
+        arrays = {f"basis_{i}": np.load(os.path.join(stage, f"basis_{i}.npy"),
+                                        mmap_mode="r") for i in want}
+        shape = np.asarray(next(iter(masks.values()))).shape
+        lab = np.zeros(shape, np.uint8)
+        for i, m in masks.items():
+            lab[np.asarray(m, bool)] = i
+        arrays["labels"] = lab
+        fa_cache.store(spec, arrays, root=root)
+        del arrays
+        import shutil
+        shutil.rmtree(stage, ignore_errors=True)
+    barrier()
+    return out, key

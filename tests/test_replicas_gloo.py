@@ -1,9 +1,10 @@
 """The multi-GPU path on CPU: two gloo ranks (127.0.0.1) exercise the
 replica logic the benchmark and the sharded basis door use -- the barrier,
 the slowest rank's time, whole-job throughput, and the dealing of
-independent bases so every basis belongs to exactly one rank.  No GPU:
-the basis door is replaced by a recorder of what each rank was asked to
-solve."""
+independent bases so every basis belongs to exactly one rank, and the
+sharded mixed-precision batch whose ranks' bases rank 0 assembles into one
+cache entry.  No GPU: the basis door and the mixed batch are replaced by
+recorders of what each rank was asked to solve."""
 import os
 import socket
 
@@ -17,7 +18,7 @@ def _free_port():
         return s.getsockname()[1]
 
 
-def _rank(rank, size, port, q):
+def _rank(rank, size, port, q, cache_root):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port),
                       RANK=str(rank), WORLD_SIZE=str(size), LOCAL_RANK=str(rank))
     import numpy as np
@@ -42,17 +43,39 @@ def _rank(rank, size, port, q):
     got["mine"] = sorted(out)
     got["asked"] = asked
     got["shard_default"] = replicas.shard(masks.keys())
+    # the mixed batch, sharded, assembled into one cache entry by rank 0
+    from ion_gym_gb300.physics import mixed
+    solved = []
+
+    def fake_mixed(masks, v_basis=1e4, accuracy=1e-9, only=None, **kw):
+        solved.append(sorted(only))
+        return {i: np.full((3, 4, 5), v_basis * i / 10.0) for i in sorted(only)}
+
+    mixed.solve_bases_mixed = fake_mixed
+    deck = {}
+    for i in (4, 1, 7, 2, 9):
+        m = np.zeros((3, 4, 5), bool)
+        m[i % 3, i % 4, i % 5] = True
+        deck[i] = m
+    spec = {"name": "sharded deck", "geometry": {"n": 5}}
+    bases, key = replicas.solve_bases_mixed_sharded(deck, spec=spec,
+                                                     root=cache_root)
+    got["mixed_mine"] = sorted(bases)
+    got["mixed_solved"] = solved
+    got["key"] = key
     replicas.barrier()
     import torch.distributed as dist
     dist.destroy_process_group()
     q.put((rank, got))
 
 
-def test_two_gloo_ranks_share_the_work():
+def test_two_gloo_ranks_share_the_work(tmp_path):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    root = str(tmp_path / "cache")
+    procs = [ctx.Process(target=_rank, args=(r, 2, port, q, root))
+             for r in range(2)]
     for p in procs:
         p.start()
     res = dict(q.get(timeout=120) for _ in procs)
@@ -68,6 +91,21 @@ def test_two_gloo_ranks_share_the_work():
     assert sorted(a + b) == [1, 2, 4, 7, 9] and not set(a) & set(b)
     assert res[0]["asked"] == [a] and res[1]["asked"] == [b]
     assert res[0]["shard_default"] == a and res[1]["shard_default"] == b
+    # sharded mixed batch: each rank solved its share once; one entry holds
+    # every basis (float32 unit bases) and the labels
+    assert res[0]["mixed_solved"] == [a] and res[1]["mixed_solved"] == [b]
+    assert res[0]["mixed_mine"] == a and res[1]["mixed_mine"] == b
+    assert res[0]["key"] == res[1]["key"]
+    import numpy as np
+    from ion_gym_gb300.io import fa_cache
+    arrs, meta = fa_cache.load(res[0]["key"], root=root)
+    assert sorted(arrs) == ["basis_1", "basis_2", "basis_4", "basis_7",
+                            "basis_9", "labels"]
+    for i in (1, 2, 4, 7, 9):
+        assert arrs[f"basis_{i}"].dtype == np.float32
+        assert np.all(arrs[f"basis_{i}"] == np.float32(i / 10.0))
+        assert arrs["labels"][i % 3, i % 4, i % 5] == i
+    assert [n for n in os.listdir(root) if n.startswith(".")] == []
 
 
 def test_one_rank_is_the_identity():
