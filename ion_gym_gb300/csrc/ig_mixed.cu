@@ -1425,13 +1425,19 @@ struct Session {
   Buf<double> part, scal;
   int method = 1;            // 0: defect correction with `vcycles` cycles,
                              // 1: flexible CG preconditioned by one cycle
-  int cg_iters = 4;          // CG iterations per FP64 refinement
+  int cg_iters = 3;          // CG iterations per FP64 refinement
   int nu1 = 2, nu2 = 2, vcycles = 2, bottom_pairs = 40;
   int gamma = 1;             // 1: V-cycle, 2: W-cycle (coarse levels twice)
   float smooth_omega = 1.f;  // red-black relaxation factor of the smoother
   double resid_scale = 1.0;
   float bottom_omega = 1.f;
+  // captured refinement steps, by (batch size, direction parity)
   std::vector<std::pair<int, cudaGraphExec_t>> graphs;
+  // which direction buffer holds the search direction at the start of the
+  // next step: with an odd number of fused CG iterations a step ends in the
+  // other buffer, and the next step (a graph captured with the buffers
+  // swapped) starts there instead of copying it back
+  bool p_in_b2 = false;
   GsCfg gs_cfg;          // smoother launch shape, from the tuner
   bool gs_tuned = false;
 
@@ -1680,6 +1686,7 @@ struct Session {
     k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, f.G.n, f.pstride);
     MK(cudaMemsetAsync(xb.p, 0, f.pstride * B * 4, s));
     MK(cudaMemsetAsync(pb.p, 0, f.pstride * B * 4, s));
+    p_in_b2 = false;
     MK(cudaMemsetAsync(qb.p, 0, f.pstride * B * 4, s));
     MK(cudaMemsetAsync(scal.p, 0, 4 * B * 8, s));
   }
@@ -1687,14 +1694,14 @@ struct Session {
   // cg_iters preconditioned iterations, then the reliable update: the FP32
   // correction is added to the FP64 potential, whose exact FP64 residual
   // replaces the carried one (the search direction is kept)
-  void cg_enqueue() {
+  void cg_enqueue(bool from_b2) {
     MLevel& f = lv[0];
     const uint32_t n = (uint32_t)f.pstride;
     const dim3 gv(nblk(n), B);
     const unsigned nb4 = std::min(nblk(f.G.csz / 4), kCgBlocks);
     const unsigned nbd = std::min(nblk(n / 4), kCgBlocks);
-    float* pcur = pb.p;
-    float* pnext = pb2.p;
+    float* pcur = from_b2 ? pb2.p : pb.p;
+    float* pnext = from_b2 ? pb.p : pb2.p;
     for (int it = 0; it < cg_iters; it++) {
       vcycle(0, true);  // z = f.e
       k_cg_dot<<<dim3(nbd, B), kT, 0, s>>>(f.e.p, qb.p, part.p, f.pstride, n);
@@ -1724,30 +1731,34 @@ struct Session {
     k_update64_8<<<dim3(nblk(f.G.csz / 4), B), kT, 0, s>>>(
         phi.p, fixed.p, cg_iters > 1 ? xb.p : nullptr, f.G, dmax.p, f.G.n, f.pstride, pcur,
         scal.p);
-    // the next step (a replay of this graph) starts from pb
-    if (pcur != pb.p)
-      MK(cudaMemcpyAsync(pb.p, pcur, f.pstride * B * 4, cudaMemcpyDeviceToDevice, s));
     k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, f.G.n, f.pstride);
   }
 
+  // a step ends with the direction in the other buffer when the fused CG
+  // runs an odd number of iterations
+  bool step_swaps() const { return method == 1 && fuse_dir() && (cg_iters & 1); }
+
   void step() {
+    const bool from_b2 = method == 1 && p_in_b2;
+    const int key = 2 * B + (from_b2 ? 1 : 0);
     cudaGraphExec_t exec = nullptr;
     for (auto& g : graphs)
-      if (g.first == B) exec = g.second;
+      if (g.first == key) exec = g.second;
     if (!exec) {
       if (!gs_tuned) tune_gs(B);
       cudaGraph_t graph;
       MK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
       if (method == 1)
-        cg_enqueue();
+        cg_enqueue(from_b2);
       else
         step_enqueue();
       MK(cudaStreamEndCapture(s, &graph));
       MK(cudaGraphInstantiate(&exec, graph, 0));
       MK(cudaGraphDestroy(graph));
-      graphs.push_back({B, exec});
+      graphs.push_back({key, exec});
     }
     MK(cudaGraphLaunch(exec, s));
+    if (step_swaps()) p_in_b2 = !p_in_b2;
   }
 
   // kernel launches of one cycle on level l (memsets are not kernels)
@@ -1850,7 +1861,7 @@ int ig_mixed_open(const uint8_t* metal, long nx, long ny, long nz,
                   int max_problems, int stencil, int nu1, int nu2, int vcycles,
                   void** handle) {
   return ig_mixed_open_ex(metal, nx, ny, nz, max_problems, stencil, nu1, nu2,
-                          vcycles, 1, 1.0, 1, 4, handle);
+                          vcycles, 1, 1.0, 1, 3, handle);
 }
 
 int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,

@@ -33,7 +33,7 @@ class Request:
     __slots__ = ("rid", "masks", "v_basis", "accuracy", "arrival", "start",
                  "end", "future", "key", "bytes", "n_bases", "shape")
 
-    def __init__(self, rid, masks, v_basis, accuracy, bytes_fn):
+    def __init__(self, rid, masks, v_basis, accuracy, bytes_fn, key=None):
         self.rid = rid
         self.masks = masks
         self.v_basis = v_basis
@@ -44,13 +44,22 @@ class Request:
         first = np.asarray(next(iter(masks.values())), bool)
         self.shape = first.shape
         self.n_bases = len(masks)
-        metal = np.zeros(self.shape, bool)
-        for m in masks.values():
-            metal |= np.asarray(m, bool)
-        h = hashlib.sha256(np.packbits(metal).tobytes())
-        h.update(repr((self.shape, self.n_bases)).encode())
-        self.key = h.hexdigest()
+        if key is None:
+            h = hashlib.sha256(np.packbits(metal_of(masks, self.shape)).tobytes())
+            h.update(repr((self.shape, self.n_bases)).encode())
+            key = h.hexdigest()
+        else:
+            key = f"{key}|{self.shape}|{self.n_bases}"
+        self.key = key
         self.bytes = bytes_fn(self.shape, self.n_bases)
+
+
+def metal_of(masks, shape):
+    """The union of a deck's electrode masks."""
+    metal = np.zeros(shape, bool)
+    for m in masks.values():
+        metal |= np.asarray(m, bool)
+    return metal
 
 
 class FieldServer:
@@ -100,13 +109,18 @@ class FieldServer:
             t.start()
 
     # -------------------------------------------------------------- API
-    def submit(self, masks, v_basis=1e4, accuracy=1e-9):
-        """Queue a deck; returns a Future of {index: basis float64}."""
+    def submit(self, masks, v_basis=1e4, accuracy=1e-9, key=None):
+        """Queue a deck; returns a Future of {index: basis float64}.
+        key: the caller's identity of the deck's geometry (the same key for
+        the same metal, e.g. its cache key); without it the server hashes
+        the union of the masks, which costs a pass over every mask on the
+        submitting thread."""
+        r = Request(None, dict(sorted(masks.items())), v_basis, accuracy,
+                    self._bytes_fn, key=key)
         with self._cv:
             if self._closed:
                 raise RuntimeError("server is closed")
-            r = Request(self._next, dict(sorted(masks.items())), v_basis,
-                        accuracy, self._bytes_fn)
+            r.rid = self._next
             self._next += 1
             if r.bytes > self.budget:
                 r.future.set_exception(MemoryError(
@@ -173,10 +187,7 @@ class FieldServer:
             held = sess.nbytes if sess is not None else r.bytes
             try:
                 if sess is None:
-                    metal = np.zeros(r.shape, bool)
-                    for m in r.masks.values():
-                        metal |= np.asarray(m, bool)
-                    sess = self._factory(metal, r.n_bases)
+                    sess = self._factory(metal_of(r.masks, r.shape), r.n_bases)
                 if self.results == "device":
                     import torch
                     out = torch.empty((r.n_bases,) + r.shape, dtype=torch.float64,

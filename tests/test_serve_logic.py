@@ -97,3 +97,21 @@ def test_unknown_results_kind_is_refused():
     with pytest.raises(ValueError, match="results"):
         FieldServer(workers=1, hbm_budget=100, device=None,
                     session_factory=FakeSession, results="disk")
+
+
+def test_caller_keys_identify_geometries():
+    """A deck submitted with the caller's geometry key is matched to a
+    resident session by that key (no pass over its masks); another key is
+    another geometry, and keyed and unkeyed submissions do not mix."""
+    srv = _server(workers=1, budget=1000)
+    a, b = _deck(1, 2), _deck(2, 2)
+    srv.submit(a, key="deck-a").result(timeout=10)
+    srv.submit(a, key="deck-a").result(timeout=10)
+    assert len(FakeSession.opened) == 1
+    srv.submit(b, key="deck-b").result(timeout=10)
+    assert len(FakeSession.opened) == 2
+    srv.submit(a).result(timeout=10)           # hashed key: a new session
+    assert len(FakeSession.opened) == 3
+    srv.submit(a).result(timeout=10)
+    assert len(FakeSession.opened) == 3
+    srv.close()
