@@ -193,6 +193,12 @@ void ig_mixed_close(void *handle);
  * bytes (6.5 B per node and problem). */
 int ig_mixed_time_gs(void *handle, int n_problems, int pairs,
                      double *ms_per_launch, double *bytes_per_launch);
+/* Algorithmic DRAM bytes of one refinement step of the session for
+ * n_problems problems: every kernel's inputs read once and outputs written
+ * once, summed over the captured step (all levels).  A step's time over
+ * this gives the whole step's achieved bandwidth.  No reference
+ * counterpart (a measurement aid). */
+int ig_mixed_step_bytes(void *handle, int n_problems, double *bytes_out);
 /* Checks the fused kernels of the mixed path against the separate launches
  * they replace, on the state the session's last solve left (right-hand
  * sides, corrections, direction): mismatches[0] = the first Gauss-Seidel

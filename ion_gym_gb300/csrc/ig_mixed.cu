@@ -1771,6 +1771,56 @@ struct Session {
     return n;
   }
 
+  // Algorithmic DRAM bytes of one cycle on level l, per problem: the bytes
+  // each kernel must move (its inputs read once, its outputs written once),
+  // as the kernel table of the design notes counts them.
+  double cycle_bytes(size_t l, bool zero) const {
+    const MLevel& a = lv[l];
+    const double n = (double)a.G.n;
+    if (l + 1 == lv.size()) return 9.0 * n;            // g, mask in; e out
+    double b = 0.0;
+    int q0 = 0;
+    if (zero && fuse_zero_pair(a)) {
+      b += 9.0 * n;
+      q0 = 1;
+    } else if (zero) {
+      b += 4.0 * n;                                     // memset of e
+    }
+    b += 2.0 * (nu1 - q0) * 6.5 * n;                    // half-sweeps
+    const double nc = (double)lv[l + 1].G.n;
+    if (nu1 > 0 && smooth_omega == 1.f)
+      b += 8.5 * n + 2.0 * n + 4.0 * nc;                // colour-0 residual, restriction
+    else
+      b += 13.0 * n + 4.0 * n + 4.0 * nc;
+    const int reps = (l + 2 < lv.size()) ? gamma : 1;
+    for (int q = 0; q < reps; q++) b += cycle_bytes(l + 1, q == 0);
+    const bool one = nu2 >= 1 && smooth_omega == 1.f;
+    b += (one ? 4.5 : 9.0) * n;                         // prolongation
+    b += 2.0 * nu2 * 6.5 * n;
+    return b;
+  }
+
+  // Algorithmic bytes of one refinement step for nb problems.
+  double step_bytes(int nb) const {
+    const double n = (double)lv[0].G.n;
+    double b = 0.0;
+    if (method == 1) {
+      for (int it = 0; it < cg_iters; it++) {
+        b += cycle_bytes(0, true);
+        b += 8.0 * n;                                   // <z, q>
+        b += (fuse_dir() ? 21.0 : 33.0) * n;            // direction, L p
+        if (it == 0 && cg_iters > 1) b += 20.0 * n;      // x = a p, g += a q
+        else if (it + 1 < cg_iters) b += 24.0 * n;
+      }
+      b += (cg_iters > 1 ? 25.0 : 21.0) * n;            // phi += x + a p
+    } else {
+      for (int v = 0; v < vcycles; v++) b += cycle_bytes(0, v == 0);
+      b += 21.0 * n;                                    // phi += e
+    }
+    b += 13.0 * n;                                      // FP64 residual
+    return b * nb;
+  }
+
   long launches_per_step() const {
     // per iteration: dot, two reductions, direction + L p (one launch when
     // fused) and, on all but the last, the CG update; then update64, resid64
@@ -1912,6 +1962,17 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
 }
 
 void ig_mixed_close(void* handle) { delete static_cast<Session*>(handle); }
+
+int ig_mixed_step_bytes(void* handle, int n_problems, double* bytes_out) {
+  set_last_error("");
+  Session* S = static_cast<Session*>(handle);
+  if (!S || n_problems < 1 || n_problems > S->bmax || !bytes_out) {
+    set_last_error("bad session, problem count or output pointer");
+    return IG_BAD_ARG;
+  }
+  *bytes_out = S->step_bytes(n_problems);
+  return IG_OK;
+}
 
 int ig_mixed_time_gs(void* handle, int n_problems, int pairs, double* ms_per_launch,
                      double* bytes_per_launch) {

@@ -150,6 +150,16 @@ class MixedSession:
         self.last_steps = int(steps.value)
         return phi
 
+    def step_bytes(self, n_problems=None):
+        """Algorithmic DRAM bytes of one refinement step for n_problems
+        problems (default: the session's maximum): every kernel's inputs
+        read once and outputs written once, over all levels."""
+        b = ctypes.c_double(0.0)
+        n = self.max_problems if n_problems is None else int(n_problems)
+        st = _lib.lib().ig_mixed_step_bytes(self._h, n, ctypes.byref(b))
+        _lib.check(st, "MixedSession.step_bytes")
+        return float(b.value)
+
     def _mask_stage(self, B):
         st = getattr(self, "_stage", None)
         if st is None or st.shape[0] < B:
