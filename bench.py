@@ -724,8 +724,22 @@ def serve_rate(srv, pool, rate, duration, max_requests, fresh, ring_frac,
         else:
             src = rings if ring else boards
             plan.append(src[int(rng.integers(len(src)))])
+    import threading
     n0 = len(srv.completed)
-    futs = []
+    left = [len(arrivals)]
+    errors = []
+    cv = threading.Condition()
+
+    def done(f):
+        # the consumer takes the device result and lets it go, as a field
+        # build that reads the bases in place would
+        e = f.exception()
+        with cv:
+            if e is not None:
+                errors.append(e)
+            left[0] -= 1
+            cv.notify_all()
+
     t0 = time.perf_counter()
     for t, (kind, deck, new, key) in zip(arrivals, plan):
         dt = t0 + t - time.perf_counter()
@@ -733,10 +747,13 @@ def serve_rate(srv, pool, rate, duration, max_requests, fresh, ring_frac,
             time.sleep(dt)
         # each deck comes with its geometry's identity, as a client that
         # keys decks by their cache key submits them
-        futs.append(srv.submit(deck, key=key))
-    for f in futs:
-        f.result()
+        srv.submit(deck, key=key).add_done_callback(done)
+    with cv:
+        while left[0] > 0:
+            cv.wait(1.0)
     el = time.perf_counter() - t0
+    if errors:
+        raise errors[0]
     done = srv.completed[n0:]
     lat = [r.end - r.arrival for r in done]
     return {"offered_req_s": rate, "requests": len(done),
@@ -769,7 +786,11 @@ def run_serve(a):
             for i in range(8)]
     if a.ring_frac > 0:
         pool += [("rings", _ring_deck(s), False, f"rings{s}") for s in (0, 1)]
-    srv = FieldServer(workers=a.workers, results="device")
+    # sessions may hold 60 % of the free HBM; the rest is for the results
+    # in flight (device float64 bases) and the caching allocator
+    free, _ = torch.cuda.mem_get_info(0)
+    srv = FieldServer(workers=a.workers, results="device",
+                      hbm_budget=int(0.6 * free))
     for _, d, _, key in pool:                  # warm: resident sessions
         srv.submit(d, key=key).result()
     srv.completed.clear()

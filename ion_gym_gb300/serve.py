@@ -142,7 +142,9 @@ class FieldServer:
         self._idle.clear()
 
     def latencies(self):
-        """(queue wait, service, total) seconds of every finished request."""
+        """(queue wait, service, total) seconds of every finished request
+        (finished requests keep their timing only; results live in the
+        callers' futures)."""
         return [(r.start - r.arrival, r.end - r.start, r.end - r.arrival)
                 for r in self.completed]
 
@@ -188,20 +190,15 @@ class FieldServer:
             try:
                 if sess is None:
                     sess = self._factory(metal_of(r.masks, r.shape), r.n_bases)
-                if self.results == "device":
-                    import torch
-                    out = torch.empty((r.n_bases,) + r.shape, dtype=torch.float64,
-                                      device=f"cuda:{self.device or 0}")
-                    phi = sess.solve_bases(list(r.masks.values()), r.v_basis,
-                                           r.accuracy, out=out)
-                else:
-                    phi = sess.solve_bases(list(r.masks.values()), r.v_basis,
-                                           r.accuracy)
-                result = {i: phi[b] for b, i in enumerate(r.masks)}
-                err = None
+                result, err = self._solve(sess, r), None
             except Exception as e:     # delivered through the future
                 result, err = None, e
             r.end = time.perf_counter()
+            fut = r.future
+            # the finished request keeps only its timing: the result belongs
+            # to the caller's future (device results would otherwise stay in
+            # HBM as long as the server lives), the masks to the caller
+            r.future = r.masks = None
             with self._cv:
                 self._in_use -= held
                 if sess is not None:
@@ -213,9 +210,25 @@ class FieldServer:
                 self.completed.append(r)
                 self._cv.notify_all()
             if err is None:
-                r.future.set_result(result)
+                fut.set_result(result)
             else:
-                r.future.set_exception(err)
+                fut.set_exception(err)
+            del result, fut
+
+
+    def _solve(self, sess, r):
+        """{index: basis} of a request on its session (host or device
+        arrays as the server's results kind says)."""
+        if self.results == "device":
+            import torch
+            out = torch.empty((r.n_bases,) + r.shape, dtype=torch.float64,
+                              device=f"cuda:{self.device or 0}")
+            phi = sess.solve_bases(list(r.masks.values()), r.v_basis,
+                                   r.accuracy, out=out)
+        else:
+            phi = sess.solve_bases(list(r.masks.values()), r.v_basis,
+                                   r.accuracy)
+        return {i: phi[b] for b, i in enumerate(r.masks)}
 
 
 def poisson_schedule(rate, duration, seed=0):

@@ -115,3 +115,21 @@ def test_caller_keys_identify_geometries():
     srv.submit(a).result(timeout=10)
     assert len(FakeSession.opened) == 3
     srv.close()
+
+
+def test_finished_requests_keep_no_results():
+    """A finished request keeps its timing only: the result lives in the
+    caller's future alone (device results would otherwise stay in HBM for
+    the life of the server)."""
+    import gc
+    import weakref
+    srv = _server(workers=1, budget=1000)
+    f = srv.submit(_deck(4, 2))
+    res = f.result(timeout=10)
+    probe = weakref.ref(next(iter(res.values())).base)
+    (r,) = srv.completed
+    assert r.future is None and r.masks is None and r.end >= r.start
+    del f, res
+    gc.collect()
+    assert probe() is None
+    srv.close()
