@@ -210,12 +210,16 @@ int ig_mixed_step_bytes(void *handle, int n_problems, double *bytes_out);
  * of the colour-0 residual vs the per-node one, [5] = the CG update of a
  * refinement step's first iteration (x = alpha p) vs a zeroed x and the
  * update, and the last iteration's x += alpha p folded into the FP64
- * update vs the two kernels (potentials and step maxima) -- each the number of 32-bit words
- * that differ over every multigrid level, 0 when bit-identical.
- * Flexible-CG sessions only; no reference counterpart (a self-check of this
- * library's kernel fusion). */
+ * update vs the two kernels (potentials and step maxima), [6] = the
+ * temporally blocked pre-smoothing (1, 2 and 3 Gauss-Seidel pairs from a
+ * zero correction in one pass) vs a zeroed correction and the separate
+ * half-sweeps, [7] = the blocked post-smoothing (colours 1, 0, ... into a
+ * second array) vs the separate half-sweeps on the same input -- each the
+ * number of 32-bit words that differ over every multigrid level, 0 when
+ * bit-identical.  Flexible-CG sessions only; no reference counterpart (a
+ * self-check of this library's kernel fusion). */
 int ig_mixed_check_fused(void *handle, int n_problems,
-                         long long mismatches[6]);
+                         long long mismatches[8]);
 
 /* ig_cascadic_relres for callers that cannot allocate device memory (no
  * counterpart in the reference).  Some callers may not call cudaMalloc, or

@@ -33,6 +33,7 @@
 #include <algorithm>
 #include <atomic>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <string>
@@ -342,6 +343,211 @@ k_gs_zero_pair(float* __restrict__ e, const float* __restrict__ g,
     o[u] = mv[u] ? 0.f : (q - gv[u]) * (1.0f / 6.0f);
   }
   *reinterpret_cast<float4*>(e1 + base) = make_float4(o[0], o[1], o[2], o[3]);
+}
+
+// ---- temporal blocking: S red-black half-sweeps in one pass -----------------
+//
+// The fine level's Gauss-Seidel half-sweeps (omega 1) of one smoothing phase
+// of the V-cycle run in one launch.  With omega 1 a half-sweep of colour c
+// reads only the other colour, so S alternating half-sweeps read one colour
+// of e once, g and the mask, and write e once: 11 bytes per node for any S
+// (9 when the phase starts from e = 0), against 6.5 per half-sweep.
+//
+// A CTA owns a tile of TY rows (j) by TMG float4 groups of slots (the split
+// layout's rows, both colours) and marches through the x-planes.  Stage s
+// (1..S) updates colour c_s = C1 ^ ((s - 1) & 1) on plane t - s + 1 at
+// iteration t: each stage lags the one before by one plane, so the planes
+// i - 1, i, i + 1 of stage s - 1 that stage s reads at plane i are all
+// done.  A thread keeps one float4 position (row j, group gi) through every
+// stage: the x-neighbours of its position are its own results of the stage
+// before (a three-plane register window per stage), the y-neighbours and the
+// z-edge slots come from the neighbouring positions through shared memory,
+// where every stage publishes the plane it just computed.  Stage s reads the
+// previous iteration's publication (parity t - 1) and writes parity t, so one
+// barrier per plane orders everything.  The tile carries a halo of S rows
+// and S groups on each side, shrinking by one per stage, so the last stage
+// covers exactly the tile.  Faces reflect as in the separate kernels
+// (lo_i / hi_i in y and x, the z-face rules of nbr4).
+//
+// Every node's update is the expression of gs4_at (the same neighbour sum
+// order, (q - g) * (1/6), 0 at metal and unused slots), so the result has
+// the bits of the S separate launches (checked by ig_mixed_check_fused).
+// ZERO: the phase starts from e = 0 (colour C1 = 0 first, as the cycle's
+// zero-start pair): nothing of e is read and the first stage is -g/6.
+// Otherwise the kernel reads colour 1 - C1 of `ein` and writes both colours
+// of the result to `eout`, a different array (tiles read their halo from
+// `ein` while neighbouring tiles write their output).
+template <int S, int TY, int TMG>
+struct TbShape {
+  static constexpr int R = TY + 2 * S, GR = TMG + 2 * S, NT = R * GR;
+  static constexpr size_t smem = (size_t)S * 2 * NT * sizeof(float4);
+};
+
+__device__ __forceinline__ float4 gs_update4(float4 xm, float4 xp, float4 ym, float4 yp,
+                                             float4 zc, float z0, float z4, int p, int utop,
+                                             float4 gg, uchar4 mk) {
+  if (mk.x & mk.y & mk.z & mk.w) return make_float4(0.f, 0.f, 0.f, 0.f);
+  float z[5];
+  if (p == 0) {
+    z[0] = z0; z[1] = zc.x; z[2] = zc.y; z[3] = zc.z; z[4] = zc.w;
+  } else {
+    z[0] = zc.x; z[1] = zc.y; z[2] = zc.z; z[3] = zc.w; z[4] = z4;
+  }
+  const float sx[4] = {(xm.x + xp.x) + (ym.x + yp.x), (xm.y + xp.y) + (ym.y + yp.y),
+                       (xm.z + xp.z) + (ym.z + yp.z), (xm.w + xp.w) + (ym.w + yp.w)};
+  const float gv[4] = {gg.x, gg.y, gg.z, gg.w};
+  const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
+  float o[4];
+#pragma unroll
+  for (int u = 0; u < 4; u++) {
+    const float q = sx[u] + (z[u] + (2 * u == utop ? z[u] : z[u + 1]));
+    o[u] = mv[u] ? 0.f : (q - gv[u]) * (1.0f / 6.0f);
+  }
+  return make_float4(o[0], o[1], o[2], o[3]);
+}
+
+template <int S, bool ZERO, int C1, int TY, int TMG>
+__global__ void __launch_bounds__(TbShape<S, TY, TMG>::NT, 1)
+k_gs_tb(const float* __restrict__ ein, float* __restrict__ eout, const float* __restrict__ g,
+        const uint8_t* __restrict__ mask, SGeo G, size_t pstride) {
+  using Sh = TbShape<S, TY, TMG>;
+  constexpr int R = Sh::R, GR = Sh::GR, NT = Sh::NT;
+  extern __shared__ float4 tb_sm[];  // [stage 0..S-1][parity][NT]; stage 0 = input
+  const int tid = threadIdx.x;
+  const int r = tid / GR, q = tid - r * GR;
+  const int H4 = G.H >> 2;
+  const int ntj = (G.ny + TY - 1) / TY;
+  const int tj = (int)(blockIdx.x % (unsigned)ntj), tg = (int)(blockIdx.x / (unsigned)ntj);
+  const int j0 = tj * TY, g0 = tg * TMG;
+  const int j = j0 - S + r, gi = g0 - S + q;
+  const bool indom = j >= 0 && j < G.ny && gi >= 0 && gi < H4;
+  const int m0 = 4 * gi;
+  const size_t pb = (size_t)blockIdx.y * pstride;
+  const uint32_t rowstride = (uint32_t)G.ny * (uint32_t)G.H;
+  // shared-memory rows of the y-neighbours (faces reflect into the tile)
+  const int rlo = indom ? lo_i(j, G.ny) - (j0 - S) : r;
+  const int rhi = indom ? hi_i(j, G.ny) - (j0 - S) : r;
+  float4 cur[S], prv[S], pp[S];  // stage s outputs (s = 0: input) at planes t-s+1, t-s, t-s-1
+#pragma unroll
+  for (int s = 0; s < S; s++)
+    cur[s] = prv[s] = pp[s] = make_float4(0.f, 0.f, 0.f, 0.f);
+  const int cin = 1 - C1;  // the colour the first stage reads
+  if (!ZERO && indom) {   // plane 0 of the input
+    cur[0] = ld4(ein + pb + (size_t)cin * G.csz + (uint32_t)j * G.H + m0);
+  }
+  if (!ZERO) tb_sm[(0 * 2 + 1) * NT + tid] = cur[0];
+  __syncthreads();
+  const int last = G.nx - 1 + S - 1;
+  for (int t = 0; t <= last; t++) {
+    const int rd = (t - 1) & 1, wr = t & 1;
+    if (!ZERO) {
+      pp[0] = prv[0];
+      prv[0] = cur[0];
+      cur[0] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (indom && t + 1 < G.nx)
+        cur[0] = ld4(ein + pb + (size_t)cin * G.csz + (uint32_t)(t + 1) * rowstride +
+                     (uint32_t)j * G.H + m0);
+      tb_sm[(0 * 2 + wr) * NT + tid] = cur[0];
+    }
+    float4 out_last = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+    for (int s = 1; s <= S; s++) {
+      const int c = C1 ^ ((s - 1) & 1);
+      const int i = t - s + 1;
+      const bool act = indom && i >= 0 && i < G.nx && r >= s && r < R - s && q >= s &&
+                       q < GR - s;
+      float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (act) {
+        const uint32_t off = (uint32_t)i * rowstride + (uint32_t)j * G.H + m0;
+        const float4 gg = ld4(g + pb + (size_t)c * G.csz + off);
+        const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + (size_t)c * G.csz + off);
+        const int p = (i + j + c) & 1;
+        const int utop = G.nz - 1 - p - 2 * m0;
+        if (ZERO && s == 1) {
+          // e = 0 before the phase: colour 0 is -g/6 at free slots
+          o = make_float4(zero_start_e0(gg.x, mk.x), zero_start_e0(gg.y, mk.y),
+                          zero_start_e0(gg.z, mk.z), zero_start_e0(gg.w, mk.w));
+        } else {
+          const int sp = s - 1;
+          const float4* src = tb_sm + (size_t)(sp * 2 + rd) * NT;
+          const float4 xm = i > 0 ? pp[sp] : cur[sp];
+          const float4 xp = i < G.nx - 1 ? cur[sp] : pp[sp];
+          const float4 zc = prv[sp];
+          const float4 ym = src[rlo * GR + q];
+          const float4 yp = src[rhi * GR + q];
+          const float z0 = p == 0 ? (m0 > 0 ? src[r * GR + q - 1].w : zc.x) : 0.f;
+          const float z4 = p == 1 ? (m0 + 4 < G.H ? src[r * GR + q + 1].x : 0.f) : 0.f;
+          o = gs_update4(xm, xp, ym, yp, zc, z0, z4, p, utop, gg, mk);
+        }
+      }
+      if (s < S) {
+        pp[s] = prv[s];
+        prv[s] = cur[s];
+        cur[s] = o;
+        tb_sm[(size_t)(s * 2 + wr) * NT + tid] = o;
+      } else {
+        out_last = o;
+      }
+    }
+    // the finished plane: colour c_S from the last stage, colour c_{S-1}
+    // from the stage before (its previous plane)
+    const int io = t - S + 1;
+    if (indom && io >= 0 && r >= S && r < S + TY && q >= S && q < S + TMG) {
+      const int cS = C1 ^ ((S - 1) & 1);
+      const uint32_t off = (uint32_t)io * rowstride + (uint32_t)j * G.H + m0;
+      *reinterpret_cast<float4*>(eout + pb + (size_t)cS * G.csz + off) = out_last;
+      *reinterpret_cast<float4*>(eout + pb + (size_t)(1 - cS) * G.csz + off) = prv[S - 1];
+    }
+    __syncthreads();
+  }
+}
+
+// Launches the fused smoothing phase of S half-sweeps on level a (S = 2, 4,
+// 6).  zero: the phase starts from e = 0 (colours 0, 1, ...), writing ein
+// itself; otherwise colours 1, 0, ... from ein into eout.
+constexpr int kTbY = 8, kTbG = 16;
+
+template <int S, bool ZERO, int C1>
+void launch_tb_t(const float* ein, float* eout, const float* g, const uint8_t* mask,
+                 const SGeo& G, size_t pstride, int nb, cudaStream_t s) {
+  using Sh = TbShape<S, kTbY, kTbG>;
+  const unsigned ntj = (unsigned)((G.ny + kTbY - 1) / kTbY);
+  const unsigned ntg = (unsigned)(((G.H >> 2) + kTbG - 1) / kTbG);
+  k_gs_tb<S, ZERO, C1, kTbY, kTbG><<<dim3(ntj * ntg, nb), Sh::NT, Sh::smem, s>>>(
+      ein, eout, g, mask, G, pstride);
+}
+
+bool tb_supported(int S) { return S == 2 || S == 4 || S == 6; }
+
+template <int S, bool ZERO, int C1>
+cudaError_t tb_attr() {
+  return cudaFuncSetAttribute(k_gs_tb<S, ZERO, C1, kTbY, kTbG>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)TbShape<S, kTbY, kTbG>::smem);
+}
+
+// The blocked kernels' dynamic shared memory (above the default 48 KB) is
+// enabled once, outside any stream capture.
+cudaError_t tb_prepare() {
+  cudaError_t e = cudaSuccess;
+  for (cudaError_t x : {tb_attr<2, true, 0>(), tb_attr<4, true, 0>(), tb_attr<6, true, 0>(),
+                        tb_attr<2, false, 1>(), tb_attr<4, false, 1>(),
+                        tb_attr<6, false, 1>()})
+    if (x != cudaSuccess) e = x;
+  return e;
+}
+
+void launch_tb(int S, bool zero, const float* ein, float* eout, const float* g,
+               const uint8_t* mask, const SGeo& G, size_t pstride, int nb, cudaStream_t s) {
+  if (zero) {
+    if (S == 2) launch_tb_t<2, true, 0>(ein, eout, g, mask, G, pstride, nb, s);
+    else if (S == 4) launch_tb_t<4, true, 0>(ein, eout, g, mask, G, pstride, nb, s);
+    else launch_tb_t<6, true, 0>(ein, eout, g, mask, G, pstride, nb, s);
+  } else {
+    if (S == 2) launch_tb_t<2, false, 1>(ein, eout, g, mask, G, pstride, nb, s);
+    else if (S == 4) launch_tb_t<4, false, 1>(ein, eout, g, mask, G, pstride, nb, s);
+    else launch_tb_t<6, false, 1>(ein, eout, g, mask, G, pstride, nb, s);
+  }
 }
 
 // Number of 32-bit words that differ between a and b (a check of the fused
@@ -1389,7 +1595,7 @@ size_t session_bytes(Dims fine, int bmax) {
     // level 0: the flexible CG's correction, two direction buffers and L p
     if (d.n() == fine.n()) b += 4 * (2 * csz * 4 * (size_t)bmax);
     if (is_bottom(d)) break;
-    b += d.n() * 4 * (size_t)bmax;
+    b += std::max(d.n(), 2 * csz) * 4 * (size_t)bmax;
     d = coarse_of(d);
   }
   return b + 8 * (size_t)bmax;
@@ -1440,6 +1646,9 @@ struct Session {
   bool p_in_b2 = false;
   GsCfg gs_cfg;          // smoother launch shape, from the tuner
   bool gs_tuned = false;
+  // levels (finest first) whose smoothing phases run temporally blocked
+  // (k_gs_tb: each phase's half-sweeps in one pass); 0 = separate launches
+  int tb_levels = 1;
 
   ~Session() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
@@ -1491,12 +1700,15 @@ struct Session {
       MK(cudaMemsetAsync(L.g.p, 0, L.pstride * bmax * 4, s));
       const bool bottom = is_bottom(c);
       L.rstride = std::max<size_t>(L.G.n, L.G.csz);
-      if (!bottom) L.r.alloc(L.rstride * bmax, s);
+      // r doubles as the output array of the blocked post-smoothing (the
+      // two swap roles), so it holds a whole split correction per problem
+      if (!bottom) L.r.alloc(std::max(L.rstride, L.pstride) * bmax, s);
       lv.push_back(std::move(L));
       if (bottom) break;
       c = coarse_of(c);
     }
     bottom_omega = (float)omega_of(lv.back().d);
+    if (tb_levels > 0) MK(tb_prepare());
     phi.alloc(n * bmax, s);
     dmax.alloc(bmax, s);
     if (method == 1) {
@@ -1619,6 +1831,12 @@ struct Session {
     return nu1 >= 1 && smooth_omega == 1.f && !flat(a);
   }
 
+  // Temporally blocked smoothing on level l (k_gs_tb): grids with no
+  // size-1 axis, Gauss-Seidel (omega 1), phases of 1..3 pairs.
+  bool use_tb(size_t l) const {
+    return (int)l < tb_levels && l + 1 < lv.size() && !flat(lv[l]) && smooth_omega == 1.f;
+  }
+
   // One cycle on level l.  zero: the level's correction starts at 0 (the
   // cycle zeroes it, or its first Gauss-Seidel pair writes every slot).
   void vcycle(size_t l, bool zero) {
@@ -1630,7 +1848,11 @@ struct Session {
       return;
     }
     int q0 = 0;
-    if (zero && fuse_zero_pair(a)) {
+    if (zero && nu1 >= 1 && use_tb(l) && tb_supported(2 * nu1)) {
+      // the whole pre-smoothing from e = 0 in one pass (reads no e)
+      launch_tb(2 * nu1, true, a.e.p, a.e.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+      q0 = nu1;
+    } else if (zero && fuse_zero_pair(a)) {
       k_gs_zero_pair<<<dim3(nblk(a.G.csz / 4), B), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G,
                                                               a.pstride);
       q0 = 1;
@@ -1663,6 +1885,12 @@ struct Session {
     const unsigned pcol = (nu2 >= 1 && smooth_omega == 1.f) ? 1u : 2u;
     launch_prolong(b, a, B, pcol);
     // post-smoothing in the reverse colour order keeps the cycle symmetric
+    if (nu2 >= 1 && use_tb(l) && tb_supported(2 * nu2)) {
+      // in one pass, from e into r, which then serves as the correction
+      launch_tb(2 * nu2, false, a.e.p, a.r.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+      std::swap(a.e, a.r);
+      return;
+    }
     for (int q = 0; q < nu2; q++)
       for (int c = 1; c >= 0; c--) launch_gs(a, c, B, smooth_omega);
   }
@@ -1762,11 +1990,18 @@ struct Session {
   }
 
   // kernel launches of one cycle on level l (memsets are not kernels)
+  bool tb_pre(size_t l, bool zero) const {
+    return zero && nu1 >= 1 && use_tb(l) && tb_supported(2 * nu1);
+  }
+  bool tb_post(size_t l) const { return nu2 >= 1 && use_tb(l) && tb_supported(2 * nu2); }
+
   long cycle_launches(size_t l, bool zero) const {
     if (l + 1 == lv.size()) return 1;
     const int reps = (l + 2 < lv.size()) ? gamma : 1;
-    long n = 2 * (nu1 + nu2) + 3;
-    if (zero && fuse_zero_pair(lv[l])) n -= 1;
+    long n = 3;                                         // residual, restriction, prolongation
+    if (tb_pre(l, zero)) n += 1;
+    else n += 2 * nu1 - ((zero && fuse_zero_pair(lv[l])) ? 1 : 0);
+    n += tb_post(l) ? 1 : 2 * nu2;
     for (int q = 0; q < reps; q++) n += cycle_launches(l + 1, q == 0);
     return n;
   }
@@ -1780,7 +2015,10 @@ struct Session {
     if (l + 1 == lv.size()) return 9.0 * n;            // g, mask in; e out
     double b = 0.0;
     int q0 = 0;
-    if (zero && fuse_zero_pair(a)) {
+    if (tb_pre(l, zero)) {
+      b += 9.0 * n;                                     // g, mask in; e out
+      q0 = nu1;
+    } else if (zero && fuse_zero_pair(a)) {
       b += 9.0 * n;
       q0 = 1;
     } else if (zero) {
@@ -1796,7 +2034,8 @@ struct Session {
     for (int q = 0; q < reps; q++) b += cycle_bytes(l + 1, q == 0);
     const bool one = nu2 >= 1 && smooth_omega == 1.f;
     b += (one ? 4.5 : 9.0) * n;                         // prolongation
-    b += 2.0 * nu2 * 6.5 * n;
+    // blocked: one colour of e, g and the mask in, e out
+    b += tb_post(l) ? 11.0 * n : 2.0 * nu2 * 6.5 * n;
     return b;
   }
 
@@ -1948,6 +2187,9 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
     S->smooth_omega = (float)std::min(1.9, std::max(0.5, smooth_omega));
     S->method = method == 0 ? 0 : 1;
     S->cg_iters = std::min(64, std::max(1, cg_iters));
+    // IG_MIXED_TB_LEVELS: how many of the finest levels smooth temporally
+    // blocked (default 1; 0 = separate half-sweeps everywhere)
+    if (const char* v = std::getenv("IG_MIXED_TB_LEVELS")) S->tb_levels = std::max(0, std::atoi(v));
     // the Shortley-Weller residual with unit legs is half the ghost_linear
     // one: scale it so the correction solves the same equation
     S->resid_scale = stencil == 0 ? 1.0 : 2.0;
@@ -2010,7 +2252,7 @@ int ig_mixed_time_gs(void* handle, int n_problems, int pairs, double* ms_per_lau
   }
 }
 
-int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[6]) {
+int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) {
   set_last_error("");
   Session* S = static_cast<Session*>(handle);
   if (!S || !mismatches || n_problems < 1 || n_problems > S->bmax || S->method != 1 ||
@@ -2023,8 +2265,8 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[6]) 
     const int B = n_problems;
     cudaStream_t s = S->s;
     Buf<unsigned long long> bad;
-    bad.alloc(6, s);
-    MK(cudaMemsetAsync(bad.p, 0, 48, s));
+    bad.alloc(8, s);
+    MK(cudaMemsetAsync(bad.p, 0, 64, s));
     long launches = 0;
     auto diff = [&](const void* a, const void* b, size_t words, int slot) {
       k_count_diff<<<dim3((unsigned)((words + kT - 1) / kT), 1), kT, 0, s>>>(
@@ -2073,6 +2315,28 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[6]) 
       for (int c = 0; c < 2; c++) S->launch_gs(a, c, B, 1.f);
       diff(a.e.p, scrA, words, 0);
       launches += 3;
+      // the temporally blocked smoothing phases of 1, 2 and 3 pairs: from
+      // e = 0 (colours 0, 1, ...; over a stand-in correction) against a
+      // zeroed correction and the separate half-sweeps, and from that
+      // result (colours 1, 0, ..., into r) against the separate
+      // half-sweeps on the same input
+      for (int S2 = 2; S2 <= 6; S2 += 2) {
+        MK(cudaMemsetAsync(a.e.p, 0x7f, bytes, s));
+        launch_tb(S2, true, a.e.p, a.e.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+        MK(cudaMemcpyAsync(scrA, a.e.p, bytes, cudaMemcpyDeviceToDevice, s));
+        MK(cudaMemsetAsync(a.e.p, 0, bytes, s));
+        for (int q = 0; q < S2 / 2; q++)
+          for (int c = 0; c < 2; c++) S->launch_gs(a, c, B, 1.f);
+        diff(a.e.p, scrA, words, 6);
+        MK(cudaMemcpyAsync(scrB, a.e.p, bytes, cudaMemcpyDeviceToDevice, s));   // input
+        MK(cudaMemsetAsync(a.r.p, 0x7f, bytes, s));
+        launch_tb(S2, false, a.e.p, a.r.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+        for (int q = 0; q < S2 / 2; q++)
+          for (int c = 1; c >= 0; c--) S->launch_gs(a, c, B, 1.f);
+        diff(a.e.p, a.r.p, words, 7);
+        MK(cudaMemcpyAsync(a.e.p, scrB, bytes, cudaMemcpyDeviceToDevice, s));
+        launches += 2 + 2 * S2 + 2;
+      }
     }
     // the fused direction update + operator apply on level 0, from the
     // direction, correction and beta the solve left
@@ -2129,11 +2393,11 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[6]) 
       diff(dm.p, dm.p + B, 2 * (size_t)B, 5);
       launches += 6;
     }
-    unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
-    MK(cudaMemcpyAsync(h, bad.p, 48, cudaMemcpyDeviceToHost, s));
+    unsigned long long h[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    MK(cudaMemcpyAsync(h, bad.p, 64, cudaMemcpyDeviceToHost, s));
     MK(cudaStreamSynchronize(s));
     g_mixed_launches.fetch_add(launches);
-    for (int q = 0; q < 6; q++) mismatches[q] = (long long)h[q];
+    for (int q = 0; q < 8; q++) mismatches[q] = (long long)h[q];
     return (int)IG_OK;
   } catch (int code) {
     return code;

@@ -96,10 +96,10 @@ def test_fused_kernels_are_bit_identical(shape, seed):
     rings = [masks[i] for i in sorted(masks)]
     with MixedSession(metal, len(rings)) as s:
         s.solve_bases(rings, V, ACC)
-        bad = (ctypes.c_longlong * 6)(-1, -1, -1, -1, -1, -1)
+        bad = (ctypes.c_longlong * 8)(*([-1] * 8))
         st = _lib.lib().ig_mixed_check_fused(s._h, len(rings), bad)
         _lib.check(st, "ig_mixed_check_fused")
-    assert list(bad) == [0, 0, 0, 0, 0, 0]
+    assert list(bad) == [0] * 8
 
 
 @pytest.mark.parametrize("seed,side,n_el", [(1000, 33, 5), (1001, 65, 12),
