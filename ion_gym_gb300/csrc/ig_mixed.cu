@@ -1686,12 +1686,15 @@ struct Session {
         Buf<uint8_t> inj;
         inj.alloc(c.n(), s);
         k_coarsen_inject<<<nblk(L.G.n), kT, 0, s>>>(lv.back().nat.p, lv.back().G, inj.p, L.G);
+        MK(cudaGetLastError());
         k_coarsen_rescue<<<nblk(L.G.n), kT, 0, s>>>(lv.back().nat.p, lv.back().G, inj.p, L.nat.p,
                                                    L.G);
+        MK(cudaGetLastError());
       }
       L.mask.alloc(2 * (size_t)L.G.csz, s);
       MK(cudaMemsetAsync(L.mask.p, 1, 2 * (size_t)L.G.csz, s));  // unused slots: metal
       k_split_mask<<<nblk(L.G.n), kT, 0, s>>>(L.nat.p, L.G, L.mask.p);
+      MK(cudaGetLastError());
       L.pstride = 2 * (size_t)L.G.csz;
       L.rstride = L.G.n;
       L.e.alloc(L.pstride * bmax, s);
@@ -2175,6 +2178,9 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
     set_last_error("no CUDA device is visible");
     return IG_NO_DEVICE;
   }
+  // an error an earlier call on this thread left behind (and reported
+  // itself) is not this session's: start from a clean slate
+  cudaGetLastError();
   Session* S = new Session();
   try {
     MK(cudaStreamCreateWithFlags(&S->s, cudaStreamNonBlocking));
