@@ -406,8 +406,8 @@ __device__ __forceinline__ float4 gs_update4(float4 xm, float4 xp, float4 ym, fl
   return make_float4(o[0], o[1], o[2], o[3]);
 }
 
-template <int S, bool ZERO, int C1, int TY, int TMG>
-__global__ void __launch_bounds__(TbShape<S, TY, TMG>::NT, 1)
+template <int S, bool ZERO, int C1, int TY, int TMG, int MINB>
+__global__ void __launch_bounds__(TbShape<S, TY, TMG>::NT, MINB)
 k_gs_tb(const float* __restrict__ ein, float* __restrict__ eout, const float* __restrict__ g,
         const uint8_t* __restrict__ mask, SGeo G, size_t pstride) {
   using Sh = TbShape<S, TY, TMG>;
@@ -450,6 +450,24 @@ k_gs_tb(const float* __restrict__ ein, float* __restrict__ eout, const float* __
       tb_sm[(0 * 2 + wr) * NT + tid] = cur[0];
     }
     float4 out_last = make_float4(0.f, 0.f, 0.f, 0.f);
+    // every stage's right-hand side and mask of this iteration, issued
+    // together before any stage computes (they depend on nothing computed)
+    float4 gq[S];
+    uchar4 mq[S];
+#pragma unroll
+    for (int s = 1; s <= S; s++) {
+      const int c = C1 ^ ((s - 1) & 1);
+      const int i = t - s + 1;
+      const bool act = indom && i >= 0 && i < G.nx && r >= s && r < R - s && q >= s &&
+                       q < GR - s;
+      gq[s - 1] = make_float4(0.f, 0.f, 0.f, 0.f);
+      mq[s - 1] = make_uchar4(1, 1, 1, 1);
+      if (act) {
+        const uint32_t off = (uint32_t)i * rowstride + (uint32_t)j * G.H + m0;
+        gq[s - 1] = ld4(g + pb + (size_t)c * G.csz + off);
+        mq[s - 1] = *reinterpret_cast<const uchar4*>(mask + (size_t)c * G.csz + off);
+      }
+    }
 #pragma unroll
     for (int s = 1; s <= S; s++) {
       const int c = C1 ^ ((s - 1) & 1);
@@ -458,9 +476,8 @@ k_gs_tb(const float* __restrict__ ein, float* __restrict__ eout, const float* __
                        q < GR - s;
       float4 o = make_float4(0.f, 0.f, 0.f, 0.f);
       if (act) {
-        const uint32_t off = (uint32_t)i * rowstride + (uint32_t)j * G.H + m0;
-        const float4 gg = ld4(g + pb + (size_t)c * G.csz + off);
-        const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + (size_t)c * G.csz + off);
+        const float4 gg = gq[s - 1];
+        const uchar4 mk = mq[s - 1];
         const int p = (i + j + c) & 1;
         const int utop = G.nz - 1 - p - 2 * m0;
         if (ZERO && s == 1) {
@@ -505,15 +522,18 @@ k_gs_tb(const float* __restrict__ ein, float* __restrict__ eout, const float* __
 // Launches the fused smoothing phase of S half-sweeps on level a (S = 2, 4,
 // 6).  zero: the phase starts from e = 0 (colours 0, 1, ...), writing ein
 // itself; otherwise colours 1, 0, ... from ein into eout.
-constexpr int kTbY = 8, kTbG = 16;
+// Tile of each phase length: TY rows by TG float4 groups, MB CTAs per SM.
+template <int S> struct TbTile { static constexpr int TY = 8, TG = 8, MB = 2; };
+template <> struct TbTile<6> { static constexpr int TY = 8, TG = 16, MB = 1; };
 
 template <int S, bool ZERO, int C1>
 void launch_tb_t(const float* ein, float* eout, const float* g, const uint8_t* mask,
                  const SGeo& G, size_t pstride, int nb, cudaStream_t s) {
-  using Sh = TbShape<S, kTbY, kTbG>;
-  const unsigned ntj = (unsigned)((G.ny + kTbY - 1) / kTbY);
-  const unsigned ntg = (unsigned)(((G.H >> 2) + kTbG - 1) / kTbG);
-  k_gs_tb<S, ZERO, C1, kTbY, kTbG><<<dim3(ntj * ntg, nb), Sh::NT, Sh::smem, s>>>(
+  constexpr int TY = TbTile<S>::TY, TG = TbTile<S>::TG;
+  using Sh = TbShape<S, TY, TG>;
+  const unsigned ntj = (unsigned)((G.ny + TY - 1) / TY);
+  const unsigned ntg = (unsigned)(((G.H >> 2) + TG - 1) / TG);
+  k_gs_tb<S, ZERO, C1, TY, TG, TbTile<S>::MB><<<dim3(ntj * ntg, nb), Sh::NT, Sh::smem, s>>>(
       ein, eout, g, mask, G, pstride);
 }
 
@@ -521,9 +541,10 @@ bool tb_supported(int S) { return S == 2 || S == 4 || S == 6; }
 
 template <int S, bool ZERO, int C1>
 cudaError_t tb_attr() {
-  return cudaFuncSetAttribute(k_gs_tb<S, ZERO, C1, kTbY, kTbG>,
+  constexpr int TY = TbTile<S>::TY, TG = TbTile<S>::TG;
+  return cudaFuncSetAttribute(k_gs_tb<S, ZERO, C1, TY, TG, TbTile<S>::MB>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)TbShape<S, kTbY, kTbG>::smem);
+                              (int)TbShape<S, TY, TG>::smem);
 }
 
 // The blocked kernels' dynamic shared memory (above the default 48 KB) is
@@ -532,21 +553,27 @@ cudaError_t tb_prepare() {
   cudaError_t e = cudaSuccess;
   for (cudaError_t x : {tb_attr<2, true, 0>(), tb_attr<4, true, 0>(), tb_attr<6, true, 0>(),
                         tb_attr<2, false, 1>(), tb_attr<4, false, 1>(),
-                        tb_attr<6, false, 1>()})
+                        tb_attr<6, false, 1>(), tb_attr<2, false, 0>(),
+                        tb_attr<4, false, 0>(), tb_attr<6, false, 0>()})
     if (x != cudaSuccess) e = x;
   return e;
 }
 
-void launch_tb(int S, bool zero, const float* ein, float* eout, const float* g,
+// c1: the first stage's colour (0 when zero).
+void launch_tb(int S, bool zero, int c1, const float* ein, float* eout, const float* g,
                const uint8_t* mask, const SGeo& G, size_t pstride, int nb, cudaStream_t s) {
   if (zero) {
     if (S == 2) launch_tb_t<2, true, 0>(ein, eout, g, mask, G, pstride, nb, s);
     else if (S == 4) launch_tb_t<4, true, 0>(ein, eout, g, mask, G, pstride, nb, s);
     else launch_tb_t<6, true, 0>(ein, eout, g, mask, G, pstride, nb, s);
-  } else {
+  } else if (c1 == 1) {
     if (S == 2) launch_tb_t<2, false, 1>(ein, eout, g, mask, G, pstride, nb, s);
     else if (S == 4) launch_tb_t<4, false, 1>(ein, eout, g, mask, G, pstride, nb, s);
     else launch_tb_t<6, false, 1>(ein, eout, g, mask, G, pstride, nb, s);
+  } else {
+    if (S == 2) launch_tb_t<2, false, 0>(ein, eout, g, mask, G, pstride, nb, s);
+    else if (S == 4) launch_tb_t<4, false, 0>(ein, eout, g, mask, G, pstride, nb, s);
+    else launch_tb_t<6, false, 0>(ein, eout, g, mask, G, pstride, nb, s);
   }
 }
 
@@ -1649,6 +1676,7 @@ struct Session {
   // levels (finest first) whose smoothing phases run temporally blocked
   // (k_gs_tb: each phase's half-sweeps in one pass); 0 = separate launches
   int tb_levels = 1;
+  int tb_max = 6;  // half-sweeps per blocked pass (2, 4 or 6); longer phases split
 
   ~Session() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
@@ -1851,9 +1879,23 @@ struct Session {
       return;
     }
     int q0 = 0;
-    if (zero && nu1 >= 1 && use_tb(l) && tb_supported(2 * nu1)) {
-      // the whole pre-smoothing from e = 0 in one pass (reads no e)
-      launch_tb(2 * nu1, true, a.e.p, a.e.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+    if (tb_pre(l, zero)) {
+      // the pre-smoothing from e = 0 in passes of up to tb_max half-sweeps:
+      // the first reads no e and writes it in place, the others go from e
+      // into r, which then serves as the correction
+      int left = 2 * nu1;
+      bool first = true;
+      while (left > 0) {
+        const int S2 = std::min(left, tb_max);
+        if (first) {
+          launch_tb(S2, true, 0, a.e.p, a.e.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+        } else {
+          launch_tb(S2, false, 0, a.e.p, a.r.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+          std::swap(a.e, a.r);
+        }
+        first = false;
+        left -= S2;
+      }
       q0 = nu1;
     } else if (zero && fuse_zero_pair(a)) {
       k_gs_zero_pair<<<dim3(nblk(a.G.csz / 4), B), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G,
@@ -1888,10 +1930,15 @@ struct Session {
     const unsigned pcol = (nu2 >= 1 && smooth_omega == 1.f) ? 1u : 2u;
     launch_prolong(b, a, B, pcol);
     // post-smoothing in the reverse colour order keeps the cycle symmetric
-    if (nu2 >= 1 && use_tb(l) && tb_supported(2 * nu2)) {
-      // in one pass, from e into r, which then serves as the correction
-      launch_tb(2 * nu2, false, a.e.p, a.r.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
-      std::swap(a.e, a.r);
+    if (tb_post(l)) {
+      // in passes of up to tb_max half-sweeps, each from e into r, which
+      // then serves as the correction
+      for (int left = 2 * nu2; left > 0;) {
+        const int S2 = std::min(left, tb_max);
+        launch_tb(S2, false, 1, a.e.p, a.r.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+        std::swap(a.e, a.r);
+        left -= S2;
+      }
       return;
     }
     for (int q = 0; q < nu2; q++)
@@ -1993,18 +2040,17 @@ struct Session {
   }
 
   // kernel launches of one cycle on level l (memsets are not kernels)
-  bool tb_pre(size_t l, bool zero) const {
-    return zero && nu1 >= 1 && use_tb(l) && tb_supported(2 * nu1);
-  }
-  bool tb_post(size_t l) const { return nu2 >= 1 && use_tb(l) && tb_supported(2 * nu2); }
+  bool tb_pre(size_t l, bool zero) const { return zero && nu1 >= 1 && use_tb(l); }
+  bool tb_post(size_t l) const { return nu2 >= 1 && use_tb(l); }
+  int tb_passes(int stages) const { return (stages + tb_max - 1) / tb_max; }
 
   long cycle_launches(size_t l, bool zero) const {
     if (l + 1 == lv.size()) return 1;
     const int reps = (l + 2 < lv.size()) ? gamma : 1;
     long n = 3;                                         // residual, restriction, prolongation
-    if (tb_pre(l, zero)) n += 1;
+    if (tb_pre(l, zero)) n += tb_passes(2 * nu1);
     else n += 2 * nu1 - ((zero && fuse_zero_pair(lv[l])) ? 1 : 0);
-    n += tb_post(l) ? 1 : 2 * nu2;
+    n += tb_post(l) ? tb_passes(2 * nu2) : 2 * nu2;
     for (int q = 0; q < reps; q++) n += cycle_launches(l + 1, q == 0);
     return n;
   }
@@ -2019,7 +2065,8 @@ struct Session {
     double b = 0.0;
     int q0 = 0;
     if (tb_pre(l, zero)) {
-      b += 9.0 * n;                                     // g, mask in; e out
+      // g, mask in, e out; the later passes read one colour of e too
+      b += 9.0 * n + 11.0 * n * (tb_passes(2 * nu1) - 1);
       q0 = nu1;
     } else if (zero && fuse_zero_pair(a)) {
       b += 9.0 * n;
@@ -2038,7 +2085,7 @@ struct Session {
     const bool one = nu2 >= 1 && smooth_omega == 1.f;
     b += (one ? 4.5 : 9.0) * n;                         // prolongation
     // blocked: one colour of e, g and the mask in, e out
-    b += tb_post(l) ? 11.0 * n : 2.0 * nu2 * 6.5 * n;
+    b += tb_post(l) ? 11.0 * n * tb_passes(2 * nu2) : 2.0 * nu2 * 6.5 * n;
     return b;
   }
 
@@ -2196,6 +2243,9 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
     // IG_MIXED_TB_LEVELS: how many of the finest levels smooth temporally
     // blocked (default 1; 0 = separate half-sweeps everywhere)
     if (const char* v = std::getenv("IG_MIXED_TB_LEVELS")) S->tb_levels = std::max(0, std::atoi(v));
+    // IG_MIXED_TB_MAX: half-sweeps per blocked pass (2, 4 or 6)
+    if (const char* v = std::getenv("IG_MIXED_TB_MAX"))
+      S->tb_max = std::min(6, std::max(2, std::atoi(v) & ~1));
     // the Shortley-Weller residual with unit legs is half the ghost_linear
     // one: scale it so the correction solves the same equation
     S->resid_scale = stencil == 0 ? 1.0 : 2.0;
@@ -2326,22 +2376,31 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
       // zeroed correction and the separate half-sweeps, and from that
       // result (colours 1, 0, ..., into r) against the separate
       // half-sweeps on the same input
+      MK(tb_prepare());
       for (int S2 = 2; S2 <= 6; S2 += 2) {
         MK(cudaMemsetAsync(a.e.p, 0x7f, bytes, s));
-        launch_tb(S2, true, a.e.p, a.e.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+        launch_tb(S2, true, 0, a.e.p, a.e.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
         MK(cudaMemcpyAsync(scrA, a.e.p, bytes, cudaMemcpyDeviceToDevice, s));
         MK(cudaMemsetAsync(a.e.p, 0, bytes, s));
         for (int q = 0; q < S2 / 2; q++)
           for (int c = 0; c < 2; c++) S->launch_gs(a, c, B, 1.f);
         diff(a.e.p, scrA, words, 6);
         MK(cudaMemcpyAsync(scrB, a.e.p, bytes, cudaMemcpyDeviceToDevice, s));   // input
+        // continuing colours 0, 1, ... (a later pre-smoothing pass)
         MK(cudaMemsetAsync(a.r.p, 0x7f, bytes, s));
-        launch_tb(S2, false, a.e.p, a.r.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+        launch_tb(S2, false, 0, a.e.p, a.r.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
+        for (int q = 0; q < S2 / 2; q++)
+          for (int c = 0; c < 2; c++) S->launch_gs(a, c, B, 1.f);
+        diff(a.e.p, a.r.p, words, 6);
+        MK(cudaMemcpyAsync(a.e.p, scrB, bytes, cudaMemcpyDeviceToDevice, s));
+        // colours 1, 0, ... (post-smoothing)
+        MK(cudaMemsetAsync(a.r.p, 0x7f, bytes, s));
+        launch_tb(S2, false, 1, a.e.p, a.r.p, a.g.p, a.mask.p, a.G, a.pstride, B, s);
         for (int q = 0; q < S2 / 2; q++)
           for (int c = 1; c >= 0; c--) S->launch_gs(a, c, B, 1.f);
         diff(a.e.p, a.r.p, words, 7);
         MK(cudaMemcpyAsync(a.e.p, scrB, bytes, cudaMemcpyDeviceToDevice, s));
-        launches += 2 + 2 * S2 + 2;
+        launches += 4 + 4 * S2 + 3;
       }
     }
     // the fused direction update + operator apply on level 0, from the
