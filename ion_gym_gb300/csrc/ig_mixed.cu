@@ -1674,8 +1674,12 @@ struct Session {
   GsCfg gs_cfg;          // smoother launch shape, from the tuner
   bool gs_tuned = false;
   // levels (finest first) whose smoothing phases run temporally blocked
-  // (k_gs_tb: each phase's half-sweeps in one pass); 0 = separate launches
-  int tb_levels = 1;
+  // (k_gs_tb: each phase's half-sweeps in one pass); 0 = separate launches.
+  // Off by default: on the benchmark decks the blocked passes measured
+  // slower than the separate half-sweeps (ring stack 77-86 against 126
+  // solves/s; each plane of the march waits on a barrier and on loads that
+  // one or two CTAs per SM cannot hide), although they move fewer bytes.
+  int tb_levels = 0;
   int tb_max = 6;  // half-sweeps per blocked pass (2, 4 or 6); longer phases split
 
   ~Session() {
@@ -2241,7 +2245,7 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
     S->method = method == 0 ? 0 : 1;
     S->cg_iters = std::min(64, std::max(1, cg_iters));
     // IG_MIXED_TB_LEVELS: how many of the finest levels smooth temporally
-    // blocked (default 1; 0 = separate half-sweeps everywhere)
+    // blocked (default 0: separate half-sweeps everywhere)
     if (const char* v = std::getenv("IG_MIXED_TB_LEVELS")) S->tb_levels = std::max(0, std::atoi(v));
     // IG_MIXED_TB_MAX: half-sweeps per blocked pass (2, 4 or 6)
     if (const char* v = std::getenv("IG_MIXED_TB_MAX"))
