@@ -757,6 +757,7 @@ def serve_rate(srv, pool, rate, duration, max_requests, fresh, ring_frac,
     done = srv.completed[n0:]
     lat = [r.end - r.arrival for r in done]
     return {"offered_req_s": rate, "requests": len(done),
+            "arrived_req_s": len(arrivals) / max(arrivals[-1], 1e-9) if arrivals else 0.0,
             "completed_req_s": len(done) / el,
             "p50_ms": 1e3 * percentile(lat, 50), "p99_ms": 1e3 * percentile(lat, 99),
             "queue_p50_ms": 1e3 * percentile([r.start - r.arrival for r in done], 50),
@@ -774,8 +775,8 @@ def run_serve(a):
     geometries, HBM admission, bases kept in HBM); a fraction of the
     requests are fresh geometries.  Swept over the offered rates `--rates`,
     p50/p99 latency beside throughput per rate; `value` is the highest
-    completed rate, the knee the last offered rate served at >= 95 % with
-    p99 under 1 s."""
+    completed rate, the knee the highest offered rate served without a
+    backlog (p99 under 1 s, median queueing no longer than service)."""
     import torch
     from ion_gym_gb300.serve import FieldServer
     torch.cuda.set_device(0)
@@ -807,10 +808,15 @@ def run_serve(a):
     el = time.perf_counter() - t0
     ck = clocks.stop()
     srv.close()
+    # the knee: the highest offered rate (with every lower one) served
+    # without a backlog -- p99 under 1 s and the median request queued no
+    # longer than it was served
     knee = None
-    for r in rows:
-        if r["completed_req_s"] >= 0.95 * r["offered_req_s"] and r["p99_ms"] < 1000:
+    for r in sorted(rows, key=lambda r: r["offered_req_s"]):
+        if r["p99_ms"] < 1000 and r["queue_p50_ms"] <= r["service_p50_ms"]:
             knee = r["offered_req_s"]
+        else:
+            break
     best = max(rows, key=lambda r: r["completed_req_s"])
     print(json.dumps({
         "metric": METRIC, "value": best["completed_req_s"], "unit": "requests/s",
