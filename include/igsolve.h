@@ -141,8 +141,11 @@ int ig_cascadic_relres(const uint8_t *fixed, const double *val, long nx,
  * on masks[b] (n_bases stacked (nx,ny,nz) uint8 masks) and 0 on the rest of
  * the metal.  Flexible conjugate gradients on the FP32 correction,
  * preconditioned by one FP32 red-black multigrid V-cycle (nu1/nu2
- * Gauss-Seidel pairs), refine the FP64 potential, whose residual is the
- * reference's fine operator with theta None (formed exactly); a basis is
+ * Gauss-Seidel pairs), refine the potential, held in 64-bit fixed point
+ * (units of 2^-56 of the largest Dirichlet magnitude, |values| in
+ * [2^-61, 2^60), else IG_BAD_ARG) and returned as float64 with the Dirichlet
+ * values exact at the metal; its residual is the reference's fine operator
+ * with theta None, an exact integer sum; a basis is
  * done when the geometric tail d * rho / (1 - rho) of its last refinement
  * step d is below `acc` (absolute, volts), rho being 3 x the larger of the
  * last two observed step ratios.  Out: phi (n_bases x n float64), refinement steps, and

@@ -5,16 +5,17 @@
 // bases of a deck, or B voltage sets on one geometry), each solved to an
 // absolute accuracy `acc` in the potential:
 //
-//   phi64 <- Dirichlet values                                  (FP64, HBM)
-//   repeat:  g32 = -(float) r64(phi64)      r64: the reference's fine-level
+//   phi <- Dirichlet values     (HBM, 64-bit fixed point: units of 2^-56 of
+//                                the problem's largest Dirichlet magnitude)
+//   repeat:  g32 = -(float) r(phi)          r: the reference's fine-level
 //                                           residual (multigrid3d.py:305-354),
-//                                           formed exactly, 0 at metal
+//                                           an exact int64 sum, 0 at metal
 //            x32 = cg_iters iterations of flexible CG on A x = g (FP32,
 //                  A x = sum(nbr x) - 6 x), each preconditioned by one
 //                  multigrid V-cycle (block-ANY coarse masks, 13-point
 //                  restriction of the colour-0 residual, trilinear
 //                  prolongation, red-black Gauss-Seidel, one-CTA bottom)
-//            phi64 += x32;  stop when the geometric tail estimated from
+//            phi += x32;    stop when the geometric tail estimated from
 //                           the observed step contraction is below acc
 //                           (per problem)
 //   (method 0 replaces the CG by `vcycles` plain V-cycles per step)
@@ -536,8 +537,6 @@ void launch_tb_t(const float* ein, float* eout, const float* g, const uint8_t* m
   k_gs_tb<S, ZERO, C1, TY, TG, TbTile<S>::MB><<<dim3(ntj * ntg, nb), Sh::NT, Sh::smem, s>>>(
       ein, eout, g, mask, G, pstride);
 }
-
-bool tb_supported(int S) { return S == 2 || S == 4 || S == 6; }
 
 template <int S, bool ZERO, int C1>
 cudaError_t tb_attr() {
@@ -1123,62 +1122,35 @@ __global__ void k_split_mask(const uint8_t* __restrict__ nat, SGeo G, uint8_t* _
 
 // ---- FP64 refinement kernels (natural phi64, split g32 / e32) -----------
 
-// sum(neighbours) - 6 * centre of seven FP64 values v[0..5], v[6], times
-// (float) nscale, evaluated exactly in 64-bit fixed point and rounded once
-// to float: every value is M * 2^(e - 1075) (53-bit significand M), so with
-// emax the largest of the seven biased exponents each value is
-// (M << 6) >> (emax - e) units of 2^(emax - 1081), exact except for bits
-// below that unit (at most 7 * 2^-59 of the largest value in all -- the
-// seven FP64 additions and products of the plain expression round at about
-// 2^-53 of it each).  |M << 6| < 2^59, so the sum of six and six times the
-// centre stay below 2^62 and their difference fits int64.  GB300 issues
-// FP64 at about 1/64 of its integer rate; this takes the seven FP64
-// operations of the expression off the FP64 pipe.  Returns false (use the
-// FP64 expression) for non-finite values and for largest magnitudes outside
-// [2^-68, 2^121], where the float scaling would leave the normal range.
-__device__ __forceinline__ bool resid_fixed(const double v[7], float nscale, float& out) {
-  unsigned long long b[7];
-  int e[7];
-  int emax = 0;
-#pragma unroll
-  for (int q = 0; q < 7; q++) {
-    b[q] = static_cast<unsigned long long>(__double_as_longlong(v[q]));
-    e[q] = static_cast<int>(static_cast<unsigned>(b[q] >> 52) & 0x7ffu);
-    emax = max(emax, e[q]);
-  }
-  if (emax == 0) {  // zeros and subnormals only
-    out = 0.f;
-    return true;
-  }
-  if (emax < 955 || emax > 1144) return false;
-  long long f[7];
-#pragma unroll
-  for (int q = 0; q < 7; q++) {
-    const unsigned long long m =
-        e[q] ? ((b[q] & 0x000fffffffffffffULL) | 0x0010000000000000ULL) << 6 : 0ULL;
-    const int d = emax - e[q];
-    const long long a = d < 64 ? static_cast<long long>(m >> d) : 0LL;
-    f[q] = static_cast<long long>(b[q]) < 0 ? -a : a;
-  }
-  const long long r = (((f[0] + f[1]) + (f[2] + f[3])) + (f[4] + f[5])) - ((f[6] << 2) + (f[6] << 1));
-  if (r == 0) {
-    out = 0.f;
-    return true;
-  }
-  // r * 2^(emax - 1081), exponent field emax - 954 in 1..190
-  out = __ll2float_rn(r) * __int_as_float((emax - 954) << 23) * nscale;
-  return true;
+// ---- the refined potential in 64-bit fixed point ---------------------------
+//
+// Problem b's potential is held as integers Phi in units of
+// u_b = 2^(E_b - 56), E_b the binary exponent of its largest Dirichlet
+// magnitude (|value| < 2^E_b; E_b in [-60, 60]), so every potential the
+// refinement can reach, bounded by the Dirichlet values, is below 2^56 units
+// in magnitude and the int64 range leaves 128x headroom.  One unit is
+// 2^-56 of the largest value: finer than a float64 ulp there (2^-53).
+// Benefits: the reference's fine residual sum(nbr) - 6 phi is an exact
+// integer sum (the float64 values of the round-1 form had to be aligned to
+// a common exponent first, about 130 integer operations per node); the
+// update adds the rounded correction; the float64 potential is formed once,
+// at the end, with the Dirichlet values written exactly at the metal.
+
+// 2^k as a float (k in [-126, 127]) and as a double (k in [-1022, 1023])
+__device__ __forceinline__ float pow2f(int k) { return __int_as_float((127 + k) << 23); }
+__device__ __forceinline__ double pow2d(int k) {
+  return __longlong_as_double(static_cast<long long>(1023 + k) << 52);
 }
 
-// g32 = -(float) (scale * r64(phi)) at free nodes, 0 at metal; r64 is the
+// g32 = -(float) (scale * r(phi)) at free nodes, 0 at metal; r is the
 // reference's fine residual with theta None (kind kPlain: sum - 6 phi; the
-// Shortley-Weller form is half of it and is scaled by 2 through `scale`,
-// nscale = -(float) scale, a power of two).  The residual is formed exactly
-// (resid_fixed) and rounded once to float.
+// Shortley-Weller form is half of it and is scaled by 2 through nscale =
+// -(float) scale, a power of two).  The residual is an exact int64 sum of
+// the fixed-point potentials, rounded once to float and scaled by u_b.
 __global__ void __launch_bounds__(kT)
-k_resid64(const double* __restrict__ phi, const uint8_t* __restrict__ fixed,
-          SGeo G, float* __restrict__ g, double scale, float nscale, size_t nstride,
-          size_t pstride) {
+k_resid64(const long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
+          SGeo G, float* __restrict__ g, const int* __restrict__ fexp, float nscale,
+          size_t nstride, size_t pstride) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= G.n) return;
   const uint32_t ij = fdivu(t, G.dnz);
@@ -1187,21 +1159,18 @@ k_resid64(const double* __restrict__ phi, const uint8_t* __restrict__ fixed,
   const int j = (int)(ij - (uint32_t)i * G.dny.d);
   float out = 0.f;
   if (!fixed[t]) {
-    const double* p = phi + blockIdx.y * nstride;
+    const long long* p = phi + blockIdx.y * nstride;
     const uint32_t sx = (uint32_t)G.ny * G.nz, sy = G.nz;
     const uint32_t row = (uint32_t)i * sx + (uint32_t)j * sy;
-    double v[7];
-    v[0] = p[(uint32_t)lo_i(i, G.nx) * sx + (uint32_t)j * sy + k];
-    v[1] = p[(uint32_t)hi_i(i, G.nx) * sx + (uint32_t)j * sy + k];
-    v[2] = p[(uint32_t)i * sx + (uint32_t)lo_i(j, G.ny) * sy + k];
-    v[3] = p[(uint32_t)i * sx + (uint32_t)hi_i(j, G.ny) * sy + k];
-    v[4] = p[row + lo_i(k, G.nz)];
-    v[5] = p[row + hi_i(k, G.nz)];
-    v[6] = p[t];
-    if (!resid_fixed(v, nscale, out)) {
-      const double s = ((v[0] + v[1]) + (v[2] + v[3])) + (v[4] + v[5]);
-      out = (float)(-scale * (s - 6.0 * v[6]));
-    }
+    const long long s =
+        ((p[(uint32_t)lo_i(i, G.nx) * sx + (uint32_t)j * sy + k] +
+          p[(uint32_t)hi_i(i, G.nx) * sx + (uint32_t)j * sy + k]) +
+         (p[(uint32_t)i * sx + (uint32_t)lo_i(j, G.ny) * sy + k] +
+          p[(uint32_t)i * sx + (uint32_t)hi_i(j, G.ny) * sy + k])) +
+        (p[row + lo_i(k, G.nz)] + p[row + hi_i(k, G.nz)]);
+    const long long c = p[t];
+    const long long r = s - ((c << 2) + (c << 1));
+    out = __ll2float_rn(r) * pow2f(fexp[blockIdx.y] - 56) * nscale;
   }
   g[blockIdx.y * pstride + (size_t)scol(i, j, k) * G.csz + sidx(G, i, j, k)] = out;
 }
@@ -1223,27 +1192,27 @@ __device__ __forceinline__ double widen(float d) {
   return (double)d;
 }
 
-// phi64 += e32 at free nodes; the per-problem maximum of |e32| (exact in
-// FP64; the applied change |phi_new - phi_old| differs from it by at most
-// half an ulp of phi) goes to dmax[b] (the refinement's convergence norm,
-// the analogue of the V-cycle's full-cycle change, multigrid3d.py:702).
-// One FP64 operation per node.  Eight consecutive natural nodes
+// Phi += e32 / u_b (rounded to the nearest unit) at free nodes; the
+// per-problem maximum of |e32| (the applied change, to within half a unit)
+// goes to dmax[b] as float64 bits (the refinement's convergence norm, the
+// analogue of the V-cycle's full-cycle change, multigrid3d.py:702).  Eight
+// consecutive natural nodes
 // k0 = 8g .. 8g+7 of one row per thread: their corrections are float4 group
 // g of each colour's split row (k0 is even, so colour (i + j) & 1 holds k0,
 // k0+2, .. and the other colour k0+1, k0+3, ..), the potentials and masks
 // 64 and 8 contiguous bytes.  One block maximum per 2048 nodes.
 __global__ void __launch_bounds__(kT)
-k_update64_8(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
+k_update64_8(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
              const float* __restrict__ e, SGeo G, unsigned long long* dmax,
-             size_t nstride, size_t pstride, const float* __restrict__ p = nullptr,
-             const double* __restrict__ scal = nullptr) {
+             const int* __restrict__ fexp, size_t nstride, size_t pstride,
+             const float* __restrict__ p = nullptr, const double* __restrict__ scal = nullptr) {
   // The block's groups cover one contiguous natural range [n_lo, n_hi) (a
   // row's valid groups are consecutive and the next row starts where it
   // ends; groups past a row's end cover nothing), at most 8 kT nodes: the
   // potentials and masks of that range go through shared memory, so global
   // loads and stores are coalesced whole rows instead of 64-byte pieces per
   // thread.
-  __shared__ double sphi[kT * 8];
+  __shared__ long long sphi[kT * 8];
   __shared__ uint8_t sfix[kT * 8];
   const uint32_t ngroups = G.csz >> 2;
   const uint32_t H4 = G.dH4.d;
@@ -1255,7 +1224,8 @@ k_update64_8(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
   const uint32_t n_lo = k00 < nz ? ij0 * nz + k00 : (ij0 + 1) * nz;
   const uint32_t n_hi = k01 < nz ? min(ij1 * nz + k01 + 8, (ij1 + 1) * nz) : (ij1 + 1) * nz;
   const uint32_t span = n_hi > n_lo ? n_hi - n_lo : 0;
-  double* P = phi + blockIdx.y * nstride;
+  long long* P = phi + blockIdx.y * nstride;
+  const float to_units = pow2f(56 - fexp[blockIdx.y]);
   for (uint32_t q = threadIdx.x; q < span; q += kT) {
     sphi[q] = P[n_lo + q];
     sfix[q] = fixed[n_lo + q];
@@ -1290,7 +1260,7 @@ k_update64_8(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
       for (int u = 0; u < 8; u++) {
         if (k0 + u >= G.nz || sfix[off + u]) continue;
         const double dd = widen(ev[u]);
-        sphi[off + u] = sphi[off + u] + dd;
+        sphi[off + u] = sphi[off + u] + __float2ll_rn(ev[u] * to_units);
         unsigned long long kk =
             static_cast<unsigned long long>(__double_as_longlong(dd)) & 0x7fffffffffffffffULL;
         if (kk > 0x7ff0000000000000ULL) kk = 0x7ff0000000000000ULL;  // NaN: never converged
@@ -1303,20 +1273,60 @@ k_update64_8(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
   block_max_to(key, dmax + blockIdx.y);
 }
 
-// phi64[b] = Dirichlet values of problem b at metal, 0 elsewhere; for a
-// basis set the value is v_basis on mask b.
-__global__ void k_init_basis(double* __restrict__ phi, const uint8_t* __restrict__ masks,
-                             uint32_t n, double v, size_t nstride) {
+// Phi[b] = the Dirichlet values of problem b at metal (in units of u_b), 0
+// elsewhere; for a basis set v_basis (vfx units) on mask b.
+__global__ void k_init_basis(long long* __restrict__ phi, const uint8_t* __restrict__ masks,
+                             uint32_t n, long long vfx, size_t nstride) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= n) return;
-  phi[blockIdx.y * nstride + t] = masks[(size_t)blockIdx.y * n + t] ? v : 0.0;
+  phi[blockIdx.y * nstride + t] = masks[(size_t)blockIdx.y * n + t] ? vfx : 0LL;
 }
 
-__global__ void k_init_vals(double* __restrict__ phi, const uint8_t* __restrict__ fixed,
-                            const double* __restrict__ val, uint32_t n, size_t nstride) {
+__global__ void k_init_vals(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
+                            const double* __restrict__ val, uint32_t n, size_t nstride,
+                            const int* __restrict__ fexp) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= n) return;
-  phi[blockIdx.y * nstride + t] = fixed[t] ? val[blockIdx.y * nstride + t] : 0.0;
+  const double v = val[blockIdx.y * nstride + t];
+  phi[blockIdx.y * nstride + t] =
+      fixed[t] ? __double2ll_rn(v * pow2d(56 - fexp[blockIdx.y])) : 0LL;
+}
+
+// Per problem, the largest |Dirichlet value| at the metal, as float64 bits
+// (NaN and infinities count as the largest finite value, so the caller's
+// range check refuses them).
+__global__ void __launch_bounds__(kT)
+k_absmax_vals(const double* __restrict__ val, const uint8_t* __restrict__ fixed, uint32_t n,
+              size_t nstride, unsigned long long* out) {
+  unsigned long long key = 0;
+  for (uint32_t t = blockIdx.x * kT + threadIdx.x; t < n; t += gridDim.x * kT) {
+    if (!fixed[t]) continue;
+    unsigned long long kk =
+        static_cast<unsigned long long>(__double_as_longlong(val[blockIdx.y * nstride + t])) &
+        0x7fffffffffffffffULL;
+    if (kk >= 0x7ff0000000000000ULL) kk = 0x7fefffffffffffffULL;
+    key = max(key, kk);
+  }
+  block_max_to(key, out + blockIdx.y);
+}
+
+// In place: the float64 potential of problem b from its units (Phi * u_b,
+// one rounding when |Phi| >= 2^53), with the Dirichlet values written
+// exactly at the metal: vals (n per problem) when given, else the basis
+// set's v_basis on mask b (masks, n per problem) and 0 on the rest.
+__global__ void k_fixed_out(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
+                            const double* __restrict__ vals, const uint8_t* __restrict__ masks,
+                            double v, uint32_t n, size_t nstride,
+                            const int* __restrict__ fexp) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= n) return;
+  const size_t o = blockIdx.y * nstride + t;
+  double r;
+  if (fixed[t])
+    r = vals ? vals[o] : (masks[(size_t)blockIdx.y * n + t] ? v : 0.0);
+  else
+    r = __ll2double_rn(phi[o]) * pow2d(fexp[blockIdx.y] - 56);
+  reinterpret_cast<double*>(phi)[o] = r;
 }
 
 // ---- flexible CG on the FP32 correction (level 0, split layout) --------
@@ -1646,7 +1656,9 @@ struct Session {
   int bmax = 1;
   int B = 1;  // problems of the current call
   std::vector<MLevel> lv;
-  Buf<double> phi;
+  Buf<long long> phi;   // refined potentials, fixed point (units 2^(fexp[b] - 56))
+  Buf<int> fexp;        // per problem: the unit exponent E_b
+  Buf<unsigned long long> vmax;  // per problem: the largest |Dirichlet value|
   Buf<uint8_t> fixed;   // natural fine mask
   Buf<uint8_t> stage;   // per-call staging of basis masks
   Buf<double> vstage;   // per-call staging of Dirichlet values
@@ -1686,6 +1698,8 @@ struct Session {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
     lv.clear();
     phi.release();
+    fexp.release();
+    vmax.release();
     fixed.release();
     stage.release();
     vstage.release();
@@ -1745,6 +1759,8 @@ struct Session {
     bottom_omega = (float)omega_of(lv.back().d);
     if (tb_levels > 0) MK(tb_prepare());
     phi.alloc(n * bmax, s);
+    fexp.alloc(bmax, s);
+    vmax.alloc(bmax, s);
     dmax.alloc(bmax, s);
     if (method == 1) {
       const size_t ps = lv[0].pstride * bmax;
@@ -1954,18 +1970,20 @@ struct Session {
     MLevel& f = lv[0];
     const size_t nstride = f.G.n;
     const dim3 gn(nblk(f.G.n), B);
-    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, nstride, f.pstride);
+    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, fexp.p, (float)-resid_scale, nstride,
+                                f.pstride);
     for (int v = 0; v < vcycles; v++) vcycle(0, v == 0);
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
     k_update64_8<<<dim3(nblk(f.G.csz / 4), B), kT, 0, s>>>(phi.p, fixed.p, f.e.p, f.G, dmax.p,
-                                                         nstride, f.pstride);
+                                                         fexp.p, nstride, f.pstride);
   }
 
   // the flexible CG: once per solve, the FP64 residual and zero state
   void cg_init() {
     MLevel& f = lv[0];
     const dim3 gn(nblk(f.G.n), B);
-    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, f.G.n, f.pstride);
+    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, fexp.p, (float)-resid_scale, f.G.n,
+                                f.pstride);
     MK(cudaMemsetAsync(xb.p, 0, f.pstride * B * 4, s));
     MK(cudaMemsetAsync(pb.p, 0, f.pstride * B * 4, s));
     p_in_b2 = false;
@@ -2011,9 +2029,10 @@ struct Session {
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
     // phi += x + alpha p (x absent when the step has one iteration)
     k_update64_8<<<dim3(nblk(f.G.csz / 4), B), kT, 0, s>>>(
-        phi.p, fixed.p, cg_iters > 1 ? xb.p : nullptr, f.G, dmax.p, f.G.n, f.pstride, pcur,
-        scal.p);
-    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, resid_scale, (float)-resid_scale, f.G.n, f.pstride);
+        phi.p, fixed.p, cg_iters > 1 ? xb.p : nullptr, f.G, dmax.p, fexp.p, f.G.n, f.pstride,
+        pcur, scal.p);
+    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, fexp.p, (float)-resid_scale, f.G.n,
+                                f.pstride);
   }
 
   // a step ends with the direction in the other buffer when the fused CG
@@ -2172,9 +2191,40 @@ MixedResult run_mixed(Session& M, double acc, int max_steps) {
 }
 
 
+// The unit exponent of each problem from its largest |Dirichlet value|
+// (|value| < 2^E), uploaded to fexp; refuses magnitudes outside
+// [2^-61, 2^60) and non-finite values.
+void set_units(Session& S, const std::vector<double>& vmax) {
+  std::vector<int> e(S.B);
+  for (int b = 0; b < S.B; b++) {
+    const double m = vmax[b];
+    if (!(m < 1.152921504606846976e18)) {  // 2^60, NaN included
+      set_last_error("mixed-precision solve: a Dirichlet value is not finite or of "
+                     "magnitude 2^60 or more");
+      throw (int)IG_BAD_ARG;
+    }
+    int ex = 0;
+    if (m > 0.0) std::frexp(m, &ex);  // m = f 2^ex, f in [0.5, 1): m < 2^ex
+    if (m > 0.0 && ex < -60) {
+      set_last_error("mixed-precision solve: the Dirichlet values are all below 2^-61 in "
+                     "magnitude");
+      throw (int)IG_BAD_ARG;
+    }
+    e[b] = ex;
+  }
+  MK(cudaMemcpyAsync(S.fexp.p, e.data(), 4 * S.B, cudaMemcpyHostToDevice, S.s));
+  MK(cudaStreamSynchronize(S.s));  // e lives on this stack
+}
+
+// The float64 potentials (Dirichlet values exact at the metal: vals, or
+// v_basis on the basis masks) into phi_out.
 int finish(Session& S, const MixedResult& r, double* phi_out, int* steps_out,
-           double* dmax_out) {
-  g_mixed_launches.fetch_add(S.launches_per_step() * r.steps);
+           double* dmax_out, const double* vals, const uint8_t* masks, double v) {
+  g_mixed_launches.fetch_add(S.launches_per_step() * r.steps + 1);
+  const uint32_t n = (uint32_t)S.d.n();
+  k_fixed_out<<<dim3(nblk(n), S.B), kT, 0, S.s>>>(S.phi.p, S.fixed.p, vals, masks, v, n, n,
+                                                  S.fexp.p);
+  MK(cudaGetLastError());
   MK(cudaMemcpyAsync(phi_out, S.phi.p, S.d.n() * S.B * 8, cudaMemcpyDefault, S.s));
   MK(cudaStreamSynchronize(S.s));
   if (steps_out) *steps_out = r.steps;
@@ -2444,7 +2494,7 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
       k_cg_update<true><<<gu, kT, 0, s>>>(x, f.g.p, p, S->qb.p, S->scal.p, f.pstride, n);
       diff(x, scrA, words, 5);
       const size_t nphi = f.G.n * (size_t)B;
-      Buf<double> phi0, phi1;
+      Buf<long long> phi0, phi1;
       phi0.alloc(nphi, s);
       phi1.alloc(nphi, s);
       Buf<unsigned long long> dm;
@@ -2453,10 +2503,12 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
       MK(cudaMemcpyAsync(phi0.p, S->phi.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
       MK(cudaMemcpyAsync(scrB, x, words * 4, cudaMemcpyDeviceToDevice, s));   // x kept
       k_cg_update<false><<<gu, kT, 0, s>>>(x, f.g.p, p, S->qb.p, S->scal.p, f.pstride, n);
-      k_update64_8<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, x, f.G, dm.p, f.G.n, f.pstride);
+      k_update64_8<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, x, f.G, dm.p, S->fexp.p, f.G.n,
+                                     f.pstride);
       MK(cudaMemcpyAsync(phi1.p, S->phi.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
       MK(cudaMemcpyAsync(S->phi.p, phi0.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
-      k_update64_8<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, scrB, f.G, dm.p + B, f.G.n, f.pstride,
+      k_update64_8<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, scrB, f.G, dm.p + B, S->fexp.p,
+                                     f.G.n, f.pstride,
                                      p, S->scal.p);
       diff(S->phi.p, phi1.p, 2 * nphi, 5);
       diff(dm.p, dm.p + B, 2 * (size_t)B, 5);
@@ -2487,11 +2539,16 @@ int ig_mixed_solve_bases(void* handle, const uint8_t* masks, int n_bases,
     S->B = n_bases;
     if (!S->stage.p) S->stage.alloc(n * S->bmax, S->s);
     MK(cudaMemcpyAsync(S->stage.p, masks, n * n_bases, cudaMemcpyDefault, S->s));
+    set_units(*S, std::vector<double>(n_bases, std::fabs(v_basis)));
+    int ex = 0;
+    if (v_basis != 0.0) std::frexp(std::fabs(v_basis), &ex);
+    // v_basis in units 2^(ex - 56): exact (|v_basis| >= 2^(ex - 1))
+    const long long vfx = std::llrint(std::ldexp(v_basis, 56 - ex));
     k_init_basis<<<dim3(nblk((uint32_t)n), n_bases), kT, 0, S->s>>>(S->phi.p, S->stage.p,
-                                                                   (uint32_t)n, v_basis, n);
+                                                                   (uint32_t)n, vfx, n);
     MK(cudaGetLastError());
     const MixedResult r = run_mixed(*S, acc, max_steps);
-    return finish(*S, r, phi_out, steps_out, dmax_out);
+    return finish(*S, r, phi_out, steps_out, dmax_out, nullptr, S->stage.p, v_basis);
   } catch (int code) {
     return code;
   }
@@ -2511,11 +2568,23 @@ int ig_mixed_solve_values(void* handle, const double* vals, int n_problems,
     S->B = n_problems;
     if (!S->vstage.p) S->vstage.alloc(n * S->bmax, S->s);
     MK(cudaMemcpyAsync(S->vstage.p, vals, n * n_problems * 8, cudaMemcpyDefault, S->s));
-    k_init_vals<<<dim3(nblk((uint32_t)n), n_problems), kT, 0, S->s>>>(S->phi.p, S->fixed.p,
-                                                                     S->vstage.p, (uint32_t)n, n);
+    MK(cudaMemsetAsync(S->vmax.p, 0, 8 * (size_t)n_problems, S->s));
+    k_absmax_vals<<<dim3(std::min(nblk((uint32_t)n), 1024u), n_problems), kT, 0, S->s>>>(
+        S->vstage.p, S->fixed.p, (uint32_t)n, n, S->vmax.p);
     MK(cudaGetLastError());
+    std::vector<unsigned long long> mb(n_problems);
+    MK(cudaMemcpyAsync(mb.data(), S->vmax.p, 8 * (size_t)n_problems, cudaMemcpyDeviceToHost,
+                       S->s));
+    MK(cudaStreamSynchronize(S->s));
+    std::vector<double> vm(n_problems);
+    for (int b = 0; b < n_problems; b++) vm[b] = bits_to_double(mb[b]);
+    set_units(*S, vm);
+    k_init_vals<<<dim3(nblk((uint32_t)n), n_problems), kT, 0, S->s>>>(
+        S->phi.p, S->fixed.p, S->vstage.p, (uint32_t)n, n, S->fexp.p);
+    MK(cudaGetLastError());
+    g_mixed_launches.fetch_add(2);
     const MixedResult r = run_mixed(*S, acc, max_steps);
-    return finish(*S, r, phi_out, steps_out, dmax_out);
+    return finish(*S, r, phi_out, steps_out, dmax_out, S->vstage.p, nullptr, 0.0);
   } catch (int code) {
     return code;
   }

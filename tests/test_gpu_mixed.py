@@ -122,3 +122,26 @@ def test_uneven_batch_decks_reach_fp64_accuracy(seed, side, n_el):
     err = np.abs(got - ref).max() / span
     assert err <= ACC, (err, steps)
     assert np.array_equal(got[fixed], val[fixed])
+
+
+def test_fixed_point_units_refuse_out_of_range_values():
+    """The refined potential is held in 64-bit fixed point in units of 2^-56
+    of the problem's largest Dirichlet magnitude: values of 2^60 or more
+    (or not finite) are refused before any refinement, small and large
+    voltages within range solve to the same relative accuracy, and the
+    metal keeps its Dirichlet values exactly."""
+    from ion_gym_gb300.physics.mixed import MixedSession
+    masks = _deck((33, 29, 31), 5)
+    metal = np.zeros((33, 29, 31), bool)
+    for m in masks.values():
+        metal |= m
+    rng = np.random.default_rng(3)
+    base = np.where(metal, rng.uniform(-1.0, 1.0, metal.shape), 0.0)
+    with MixedSession(metal, 1) as s:
+        ref = s.solve_values(base, ACC, span=2.0)[0]
+        for scale in (1e-12, 1e12):
+            got = s.solve_values(base * scale, ACC, span=2.0 * scale)[0]
+            assert np.array_equal(got[metal], (base * scale)[metal])
+            assert np.abs(got / scale - ref).max() <= 4 * ACC
+        with pytest.raises(ValueError, match="2\\^60"):
+            s.solve_values(np.where(metal, 2.0 ** 61, 0.0), ACC)
