@@ -570,14 +570,17 @@ def run_uneven(a):
     """Uneven batch (BASELINE config 4): 64 seeded geometries, cubic sides
     from {33,65,97,129,193,257}, 2-16 random electrodes at U(-100,100) V,
     each solved to 1e-9 of its span by the mixed path; the geometries run
-    concurrently (one resident session and CUDA stream each, `workers` at a
-    time, largest grids first).  Each deck arrives as host buffers (metal
+    concurrently (`workers` at a time, largest grids first; each worker
+    keeps one session per grid shape, rebound to every new deck of that
+    shape, so a deck costs its mask upload and coarsening but no session
+    build).  Each deck arrives as host buffers (metal
     mask, Dirichlet values) in pinned memory, as a serving caller hands them
     over, and its potential is returned into a pinned host buffer: every
     upload, session build and download is inside the timed region.  One
     step = the whole batch of 64.  `roofline`: the algorithmic bytes of
     every refinement step of every deck over the batch's time."""
     import concurrent.futures as cf
+    import ctypes
     import torch
     from ion_gym_gb300 import _lib
     from ion_gym_gb300.workloads import random_deck
@@ -600,11 +603,29 @@ def run_uneven(a):
         span = max(float(val.max() - val.min()), 1.0)
         decks.append((pinned(fixed), pinned(val), pinned(np.zeros(val.shape)), span))
 
+    # each worker keeps one session per grid shape and rebinds it to the
+    # next deck of that shape (the new metal's masks on every level; the
+    # buffers and captured graphs stay): a new geometry costs no session
+    # build once its shape has been seen
+    import threading
+    tl = threading.local()
+    opened = []
+    olock = threading.Lock()
+
     def solve(d):
         fixed, val, out, span = d
-        with MixedSession(fixed, 1) as s:
-            s.solve_values(val, 1e-9, out=out, span=span)
-            return s.last_steps, s.last_steps * s.step_bytes(1)
+        cache = getattr(tl, "sessions", None)
+        if cache is None:
+            cache = tl.sessions = {}
+        s = cache.get(fixed.shape)
+        if s is None:
+            s = cache[fixed.shape] = MixedSession(fixed, 1)
+            with olock:
+                opened.append(s)
+        else:
+            s.rebind(fixed)
+        s.solve_values(val, 1e-9, out=out, span=span)
+        return s.last_steps, s.last_steps * s.step_bytes(1)
 
     # largest geometries first (longest-processing-time order), so the
     # small ones fill the device while the last large ones finish
@@ -625,11 +646,54 @@ def run_uneven(a):
         el = time.perf_counter() - t0
         ck = clocks.stop()
         launches = L.ig_launch_count() + _mixed_launches(L) - launches0
+    for s_ in opened:
+        s_.close()
     nodes = sum(int(sd) ** 3 for sd in sides)
     nsteps = [st for st, _ in steps]
     byts = sum(b for _, b in steps)
     achieved = byts * a.steps / el / 1e9
     peak = _peak()
+    # the kernels alone: every deck's session built beforehand and its
+    # values resident on the device, the 64 solves run by the same 12
+    # workers -- what any scheduling of these kernels (a persistent
+    # work-queue launch included) has to improve on
+    resident = None
+    try:
+        sess = [MixedSession(decks[q][0], 1) for q in order]
+        vdev = [torch.from_numpy(np.asarray(decks[q][1])).cuda() for q in order]
+        odev = [torch.empty_like(v) for v in vdev]
+
+        def solve_res(k):
+            s = sess[k]
+            st_ = ctypes.c_int(0)
+            dm = np.zeros(1)
+            rc = L.ig_mixed_solve_values(s._h, ctypes.c_void_p(vdev[k].data_ptr()), 1,
+                                         1e-9 * decks[order[k]][3], 40,
+                                         ctypes.c_void_p(odev[k].data_ptr()),
+                                         ctypes.byref(st_), dm.ctypes.data_as(ctypes.c_void_p))
+            _lib.check(rc, "uneven resident solve")
+            return st_.value * s.step_bytes(1)
+
+        with cf.ThreadPoolExecutor(workers) as ex:
+            list(ex.map(solve_res, range(len(sess))))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            rb = 0.0
+            for _ in range(a.steps):
+                rb += sum(ex.map(solve_res, range(len(sess))))
+            torch.cuda.synchronize()
+            el_r = time.perf_counter() - t0
+        resident = {"value": 64 * a.steps / el_r, "unit": "solves/s",
+                    "node_solves_s": nodes * a.steps / el_r,
+                    "achieved_gbs": rb / el_r / 1e9,
+                    "frac": rb / el_r / 1e9 / peak if peak else None,
+                    "what": "sessions resident, values on the device: the "
+                            "kernels of the 64 solves alone"}
+        for s_ in sess:
+            s_.close()
+        del sess, vdev, odev
+    except Exception as ex_:      # too little device memory for 64 sessions
+        resident = {"unavailable": str(ex_)[:200]}
     line = {
         "metric": METRIC, "value": 64 * a.steps / el, "unit": "solves/s",
         "n_gpus": 1, "steps": a.steps, "warmup": max(a.warmup, 1),
@@ -648,6 +712,7 @@ def run_uneven(a):
         "e2e": {"value": 64 * a.steps / el, "unit": "solves/s",
                 "h2d_bytes_per_step": 9 * nodes, "d2h_bytes_per_step": 8 * nodes},
         "gpu_launches": int(launches),
+        "resident": resident,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak if peak else None,
                      "traffic": None,

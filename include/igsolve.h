@@ -190,6 +190,14 @@ int ig_mixed_solve_values(void *handle, const double *vals, int n_problems,
                           double acc, int max_steps, double *phi_out,
                           int *steps_out, double *dmax_out);
 void ig_mixed_close(void *handle);
+/* Gives a session another geometry of its shape (no reference
+ * counterpart): the new metal union's masks replace the old ones on every
+ * level; the buffers, the tuned smoother shape and the captured graphs stay,
+ * so a solve on the rebound session costs no session build.  The results
+ * are those of a session opened on the new metal.  IG_BAD_ARG when the
+ * shape differs. */
+int ig_mixed_rebind(void *handle, const uint8_t *metal, long nx, long ny,
+                    long nz);
 /* Times `pairs` red-black pairs of the session's fine-level FP32
  * Gauss-Seidel kernel for n_problems problems with CUDA events on the
  * session's stream: the average launch (one colour) and its algorithmic

@@ -93,6 +93,7 @@ SIGNATURES = {
                                _d, _i, _p, _p, _p, _p]),
     "ig_mixed_time_gs": (_i, [_p, _i, _i, _pd, _pd]),
     "ig_mixed_step_bytes": (_i, [_p, _i, _pd]),
+    "ig_mixed_rebind": (_i, [_p, _p, _l, _l, _l]),
     "ig_mixed_check_fused": (_i, [_p, _i, ctypes.POINTER(ctypes.c_longlong)]),
     "ig_cascadic_relres_noalloc": (_i, [_p, _p, _l, _l, _l, _d, _l, _i, _i,
                                         _d, _p, _i, _i, _p, _pl, _pd, _pl,

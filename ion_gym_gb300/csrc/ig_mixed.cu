@@ -1716,31 +1716,44 @@ struct Session {
     }
   }
 
+  // The metal of every level: the fine mask, its coarsenings (injection
+  // with the thin-metal rescue) and their split forms, into the level
+  // buffers.  Nothing else of a session depends on the metal, so a session
+  // can take another geometry of its shape (ig_mixed_rebind) and keep its
+  // buffers, tuned smoother shape and captured graphs.
+  void load_metal(const uint8_t* metal) {
+    const size_t n = d.n();
+    MK(cudaMemcpyAsync(fixed.p, metal, n, cudaMemcpyDefault, s));
+    Buf<uint8_t> inj;
+    if (lv.size() > 1) inj.alloc(lv[1].G.n, s);
+    for (size_t l = 0; l < lv.size(); l++) {
+      MLevel& L = lv[l];
+      if (l == 0) {
+        MK(cudaMemcpyAsync(L.nat.p, fixed.p, n, cudaMemcpyDeviceToDevice, s));
+      } else {
+        const MLevel& F = lv[l - 1];
+        k_coarsen_inject<<<nblk(L.G.n), kT, 0, s>>>(F.nat.p, F.G, inj.p, L.G);
+        MK(cudaGetLastError());
+        k_coarsen_rescue<<<nblk(L.G.n), kT, 0, s>>>(F.nat.p, F.G, inj.p, L.nat.p, L.G);
+        MK(cudaGetLastError());
+      }
+      MK(cudaMemsetAsync(L.mask.p, 1, 2 * (size_t)L.G.csz, s));  // unused slots: metal
+      k_split_mask<<<nblk(L.G.n), kT, 0, s>>>(L.nat.p, L.G, L.mask.p);
+      MK(cudaGetLastError());
+    }
+    g_mixed_launches.fetch_add(3L * (long)lv.size());
+  }
+
   void build(const uint8_t* metal) {
     const size_t n = d.n();
     fixed.alloc(n, s);
-    MK(cudaMemcpyAsync(fixed.p, metal, n, cudaMemcpyDefault, s));
     Dims c = d;
     while (true) {
       MLevel L;
       L.d = c;
       L.G = sgeo(c);
       L.nat.alloc(c.n(), s);
-      if (lv.empty())
-        MK(cudaMemcpyAsync(L.nat.p, fixed.p, n, cudaMemcpyDeviceToDevice, s));
-      else {
-        Buf<uint8_t> inj;
-        inj.alloc(c.n(), s);
-        k_coarsen_inject<<<nblk(L.G.n), kT, 0, s>>>(lv.back().nat.p, lv.back().G, inj.p, L.G);
-        MK(cudaGetLastError());
-        k_coarsen_rescue<<<nblk(L.G.n), kT, 0, s>>>(lv.back().nat.p, lv.back().G, inj.p, L.nat.p,
-                                                   L.G);
-        MK(cudaGetLastError());
-      }
       L.mask.alloc(2 * (size_t)L.G.csz, s);
-      MK(cudaMemsetAsync(L.mask.p, 1, 2 * (size_t)L.G.csz, s));  // unused slots: metal
-      k_split_mask<<<nblk(L.G.n), kT, 0, s>>>(L.nat.p, L.G, L.mask.p);
-      MK(cudaGetLastError());
       L.pstride = 2 * (size_t)L.G.csz;
       L.rstride = L.G.n;
       L.e.alloc(L.pstride * bmax, s);
@@ -1756,6 +1769,7 @@ struct Session {
       if (bottom) break;
       c = coarse_of(c);
     }
+    load_metal(metal);
     bottom_omega = (float)omega_of(lv.back().d);
     if (tb_levels > 0) MK(tb_prepare());
     phi.alloc(n * bmax, s);
@@ -2314,6 +2328,26 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
 }
 
 void ig_mixed_close(void* handle) { delete static_cast<Session*>(handle); }
+
+int ig_mixed_rebind(void* handle, const uint8_t* metal, long nx, long ny, long nz) {
+  set_last_error("");
+  Session* S = static_cast<Session*>(handle);
+  if (!S || !metal) {
+    set_last_error("null argument");
+    return IG_BAD_ARG;
+  }
+  if (nx != S->d.nx || ny != S->d.ny || nz != S->d.nz) {
+    set_last_error("ig_mixed_rebind: the new metal's shape differs from the session's");
+    return IG_BAD_ARG;
+  }
+  try {
+    S->load_metal(metal);
+    MK(cudaStreamSynchronize(S->s));  // the caller may reuse its mask buffer
+  } catch (int code) {
+    return code;
+  }
+  return IG_OK;
+}
 
 int ig_mixed_step_bytes(void* handle, int n_problems, double* bytes_out) {
   set_last_error("");

@@ -150,6 +150,20 @@ class MixedSession:
         self.last_steps = int(steps.value)
         return phi
 
+    def rebind(self, metal):
+        """Give the session another geometry of the same shape: the new
+        metal union replaces the old on every multigrid level, while the
+        device buffers, the tuned smoother and the captured CUDA graphs are
+        kept -- a solve after rebind costs no session build.  Results equal
+        those of a session opened on the new metal."""
+        metal = np.asarray(metal, bool)
+        if metal.shape != self.shape:
+            raise ValueError(f"rebind: metal of shape {metal.shape}, session "
+                             f"shape {self.shape}")
+        st = _lib.lib().ig_mixed_rebind(self._h, ptr(as_mask(metal)), *self.shape)
+        _lib.check(st, "MixedSession.rebind")
+        return self
+
     def step_bytes(self, n_problems=None):
         """Algorithmic DRAM bytes of one refinement step for n_problems
         problems (default: the session's maximum): every kernel's inputs

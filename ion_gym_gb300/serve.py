@@ -9,10 +9,12 @@ device memory free up, and their kernels overlap on the device.
 Admission is by HBM footprint: a request needs ig_mixed_bytes(grid, bases)
 of device memory; it waits until the sum of the footprints of the sessions
 in use fits the budget.  Finished geometries stay resident (keyed by the
-bytes of their metal mask and basis count) and are reused by a later request
-for the same geometry -- an edited deck whose metal changed gets a new
-session; least-recently-used idle sessions are closed when the budget is
-needed.
+bytes of their metal mask and basis count, or by the caller's key) and are
+reused by a later request for the same geometry; an edited deck whose metal
+changed takes over an idle session of the same grid shape and basis count
+by rebinding it (its masks recomputed, its buffers and captured graphs
+kept), else gets a new session; least-recently-used idle sessions are
+closed when the budget is needed.
 
 Each result is computed by the same kernels in the same order whether the
 request runs alone or among others (sessions share no memory), so it is the
@@ -151,14 +153,26 @@ class FieldServer:
     # -------------------------------------------------------------- internals
     def _admit(self):
         """Pick the oldest queued request that fits; returns (request,
-        session or None).  Caller holds the lock."""
+        session or None, whether the session must be rebound to the
+        request's metal).  Caller holds the lock."""
         for i, r in enumerate(self._queue):
             sess = self._idle.pop(r.key, None)
             if sess is not None:
                 self._idle_bytes -= sess.nbytes
                 self._in_use += sess.nbytes
                 del self._queue[i]
-                return r, sess
+                return r, sess, False
+            # an idle session of the same shape and basis count takes the
+            # new geometry by rebinding (no session build)
+            for k, other in self._idle.items():
+                if (getattr(other, "shape", None) == r.shape
+                        and getattr(other, "max_problems", None) == r.n_bases
+                        and hasattr(other, "rebind")):
+                    del self._idle[k]
+                    self._idle_bytes -= other.nbytes
+                    self._in_use += other.nbytes
+                    del self._queue[i]
+                    return r, other, True
             # evict idle sessions (least recently used first) until it fits
             while (self._in_use + self._idle_bytes + r.bytes > self.budget
                    and self._idle):
@@ -168,9 +182,9 @@ class FieldServer:
             if self._in_use + self._idle_bytes + r.bytes <= self.budget:
                 self._in_use += r.bytes
                 del self._queue[i]
-                return r, None
-            return None, None       # the oldest waits: no overtaking by size
-        return None, None
+                return r, None, False
+            return None, None, False  # the oldest waits: no overtaking by size
+        return None, None, False
 
     def _worker(self):
         if self.device is not None:
@@ -181,7 +195,7 @@ class FieldServer:
                 while True:
                     if self._closed and not self._queue:
                         return
-                    r, sess = self._admit()
+                    r, sess, rebind = self._admit()
                     if r is not None:
                         break
                     self._cv.wait(0.05)
@@ -190,6 +204,8 @@ class FieldServer:
             try:
                 if sess is None:
                     sess = self._factory(metal_of(r.masks, r.shape), r.n_bases)
+                elif rebind:
+                    sess.rebind(metal_of(r.masks, r.shape))
                 result, err = self._solve(sess, r), None
             except Exception as e:     # delivered through the future
                 result, err = None, e

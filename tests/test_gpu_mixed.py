@@ -147,3 +147,30 @@ def test_fixed_point_units_refuse_out_of_range_values():
             assert np.abs(got - scale * ref).max() <= tol
         with pytest.raises(ValueError, match="2\\^60"):
             s.solve_values(np.where(metal, 2.0 ** 61, 0.0), ACC)
+
+
+def test_rebound_session_matches_a_fresh_one():
+    """A session rebound to another geometry of its shape returns the bits
+    of a session opened on that geometry (the same kernels, launch shapes
+    and captured graphs, the new masks on every level); a rebind to another
+    shape is refused."""
+    from ion_gym_gb300.physics.mixed import MixedSession
+    a = _deck((41, 37, 45), 1)
+    b = _deck((41, 37, 45), 8)
+    stack_b = [b[i] for i in sorted(b)]
+    metal_a = np.zeros((41, 37, 45), bool)
+    for m in a.values():
+        metal_a |= m
+    metal_b = np.zeros((41, 37, 45), bool)
+    for m in b.values():
+        metal_b |= m
+    with MixedSession(metal_b, len(stack_b)) as s:
+        fresh = s.solve_bases(stack_b, V, ACC).copy()
+    with MixedSession(metal_a, len(stack_b)) as s:
+        s.solve_bases([a[i] for i in sorted(a)][:len(stack_b)] +
+                      [a[sorted(a)[0]]] * (len(stack_b) - len(a)), V, ACC)
+        s.rebind(metal_b)
+        again = s.solve_bases(stack_b, V, ACC)
+        with pytest.raises(ValueError, match="shape"):
+            s.rebind(np.zeros((41, 37, 44), bool))
+    assert np.array_equal(again.view(np.uint64), fresh.view(np.uint64))

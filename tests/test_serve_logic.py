@@ -133,3 +133,35 @@ def test_finished_requests_keep_no_results():
     gc.collect()
     assert probe() is None
     srv.close()
+
+
+class RebindingSession(FakeSession):
+    rebinds = []
+
+    def __init__(self, metal, n):
+        super().__init__(metal, n)
+        self.max_problems = n
+
+    def rebind(self, metal):
+        RebindingSession.rebinds.append(np.asarray(metal).shape)
+        return self
+
+
+def test_new_geometry_of_a_resident_shape_rebinds_an_idle_session():
+    """A request whose geometry is not resident takes over an idle session
+    of the same grid shape and basis count (rebound to its metal) instead
+    of opening one; another shape or basis count opens a new session."""
+    RebindingSession.rebinds = []
+    srv = FieldServer(workers=1, hbm_budget=10000, device=None,
+                      session_factory=RebindingSession,
+                      bytes_fn=lambda shape, n: 100 * n)
+    srv.submit(_deck(1, 2)).result(timeout=10)
+    srv.submit(_deck(2, 2)).result(timeout=10)           # same shape, new metal
+    assert len(FakeSession.opened) == 1
+    assert RebindingSession.rebinds == [(6, 5, 4)]
+    srv.submit(_deck(2, 2)).result(timeout=10)           # now resident: reuse
+    assert len(FakeSession.opened) == 1 and len(RebindingSession.rebinds) == 1
+    srv.submit(_deck(3, 3)).result(timeout=10)           # other basis count
+    srv.submit(_deck(4, 2, shape=(7, 5, 4))).result(timeout=10)  # other shape
+    assert len(FakeSession.opened) == 3 and len(RebindingSession.rebinds) == 1
+    srv.close()
