@@ -1673,6 +1673,12 @@ struct Session {
   int cg_iters = 3;          // CG iterations per FP64 refinement
   int nu1 = 2, nu2 = 2, vcycles = 2, bottom_pairs = 40;
   int gamma = 1;             // 1: V-cycle, 2: W-cycle (coarse levels twice)
+  int gamma_levels = 64;     // gamma applies below the finest gamma_levels levels
+  // cycles of level l + 1 per visit of level l (the bottom is solved directly,
+  // so once is enough there)
+  int coarse_visits(size_t l) const {
+    return (l + 2 < lv.size() && (int)l < gamma_levels) ? gamma : 1;
+  }
   float smooth_omega = 1.f;  // red-black relaxation factor of the smoother
   double resid_scale = 1.0;
   float bottom_omega = 1.f;
@@ -1956,7 +1962,7 @@ struct Session {
     }
     // the coarse correction: gamma cycles on the coarse equation from 0
     // (the bottom is solved directly, so once is enough there)
-    const int reps = (l + 2 < lv.size()) ? gamma : 1;
+    const int reps = coarse_visits(l);
     for (int q = 0; q < reps; q++) vcycle(l + 1, q == 0);
     // The first post-smoothing half-sweep (colour 1, omega 1) overwrites
     // every free colour-1 slot without reading it, so only colour 0 takes
@@ -2083,7 +2089,7 @@ struct Session {
 
   long cycle_launches(size_t l, bool zero) const {
     if (l + 1 == lv.size()) return 1;
-    const int reps = (l + 2 < lv.size()) ? gamma : 1;
+    const int reps = coarse_visits(l);
     long n = 3;                                         // residual, restriction, prolongation
     if (tb_pre(l, zero)) n += tb_passes(2 * nu1);
     else n += 2 * nu1 - ((zero && fuse_zero_pair(lv[l])) ? 1 : 0);
@@ -2117,7 +2123,7 @@ struct Session {
       b += 8.5 * n + 2.0 * n + 4.0 * nc;                // colour-0 residual, restriction
     else
       b += 13.0 * n + 4.0 * n + 4.0 * nc;
-    const int reps = (l + 2 < lv.size()) ? gamma : 1;
+    const int reps = coarse_visits(l);
     for (int q = 0; q < reps; q++) b += cycle_bytes(l + 1, q == 0);
     const bool one = nu2 >= 1 && smooth_omega == 1.f;
     b += (one ? 4.5 : 9.0) * n;                         // prolongation
@@ -2311,6 +2317,10 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
     // IG_MIXED_TB_LEVELS: how many of the finest levels smooth temporally
     // blocked (default 0: separate half-sweeps everywhere)
     if (const char* v = std::getenv("IG_MIXED_TB_LEVELS")) S->tb_levels = std::max(0, std::atoi(v));
+    // IG_MIXED_GAMMA_LEVELS: the W-cycle's second coarse visit only below
+    // the finest this many levels (experiments; default all)
+    if (const char* v = std::getenv("IG_MIXED_GAMMA_LEVELS"))
+      S->gamma_levels = std::max(0, std::atoi(v));
     // IG_MIXED_TB_MAX: half-sweeps per blocked pass (2, 4 or 6)
     if (const char* v = std::getenv("IG_MIXED_TB_MAX"))
       S->tb_max = std::min(6, std::max(2, std::atoi(v) & ~1));
