@@ -43,7 +43,7 @@ enum {
 
 /* Message of the last failing call on this thread ("" if none). */
 const char *ig_last_error(void);
-/* ABI version of this header. */
+/* ABI version of this header (2: ig_mixed_open_ex takes gamma_levels). */
 int ig_abi_version(void);
 /* Number of visible CUDA devices (0 without a GPU; never fails). */
 int ig_device_count(void);
@@ -177,12 +177,15 @@ int ig_mixed_open(const uint8_t *metal, long nx, long ny, long nz,
  * refinement (the correction is then added to the FP64 potential and the
  * carried residual replaced by the exact FP64 one); method 0: plain defect
  * correction with `vcycles` cycles per refinement.  gamma 1 = V-cycle,
- * 2 = W-cycle (coarse levels cycled twice per visit); smooth_omega: the
+ * 2 = W-cycle (coarse levels cycled twice per visit); gamma_levels: the
+ * second visit only from the finest gamma_levels levels (1: a W-cycle at
+ * the top level, V below; <= 0: every level); smooth_omega: the
  * relaxation factor of the red-black smoother (1 = Gauss-Seidel). */
 int ig_mixed_open_ex(const uint8_t *metal, long nx, long ny, long nz,
                      int max_problems, int stencil, int nu1, int nu2,
-                     int vcycles, int gamma, double smooth_omega, int method,
-                     int cg_iters, void **handle);
+                     int vcycles, int gamma, int gamma_levels,
+                     double smooth_omega, int method, int cg_iters,
+                     void **handle);
 int ig_mixed_solve_bases(void *handle, const uint8_t *masks, int n_bases,
                          double v_basis, double acc, int max_steps,
                          double *phi_out, int *steps_out, double *dmax_out);

@@ -1673,7 +1673,7 @@ struct Session {
   int cg_iters = 3;          // CG iterations per FP64 refinement
   int nu1 = 2, nu2 = 2, vcycles = 2, bottom_pairs = 40;
   int gamma = 1;             // 1: V-cycle, 2: W-cycle (coarse levels twice)
-  int gamma_levels = 64;     // gamma applies below the finest gamma_levels levels
+  int gamma_levels = 64;     // the second coarse visit only from the finest levels
   // cycles of level l + 1 per visit of level l (the bottom is solved directly,
   // so once is enough there)
   int coarse_visits(size_t l) const {
@@ -2274,12 +2274,12 @@ int ig_mixed_open(const uint8_t* metal, long nx, long ny, long nz,
                   int max_problems, int stencil, int nu1, int nu2, int vcycles,
                   void** handle) {
   return ig_mixed_open_ex(metal, nx, ny, nz, max_problems, stencil, nu1, nu2,
-                          vcycles, 1, 1.0, 1, 3, handle);
+                          vcycles, 1, 0, 1.0, 1, 3, handle);
 }
 
 int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
                      int max_problems, int stencil, int nu1, int nu2,
-                     int vcycles, int gamma, double smooth_omega,
+                     int vcycles, int gamma, int gamma_levels, double smooth_omega,
                      int method, int cg_iters, void** handle) {
   set_last_error("");
   if (!handle || !metal) {
@@ -2311,16 +2311,13 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
     S->nu2 = std::max(1, nu2);
     S->vcycles = std::max(1, vcycles);
     S->gamma = std::min(2, std::max(1, gamma));
+    S->gamma_levels = gamma_levels > 0 ? gamma_levels : 64;
     S->smooth_omega = (float)std::min(1.9, std::max(0.5, smooth_omega));
     S->method = method == 0 ? 0 : 1;
     S->cg_iters = std::min(64, std::max(1, cg_iters));
     // IG_MIXED_TB_LEVELS: how many of the finest levels smooth temporally
     // blocked (default 0: separate half-sweeps everywhere)
     if (const char* v = std::getenv("IG_MIXED_TB_LEVELS")) S->tb_levels = std::max(0, std::atoi(v));
-    // IG_MIXED_GAMMA_LEVELS: the W-cycle's second coarse visit only below
-    // the finest this many levels (experiments; default all)
-    if (const char* v = std::getenv("IG_MIXED_GAMMA_LEVELS"))
-      S->gamma_levels = std::max(0, std::atoi(v));
     // IG_MIXED_TB_MAX: half-sweeps per blocked pass (2, 4 or 6)
     if (const char* v = std::getenv("IG_MIXED_TB_MAX"))
       S->tb_max = std::min(6, std::max(2, std::atoi(v) & ~1));

@@ -553,7 +553,7 @@ void ig::set_last_error(const std::string& m) { t_err = m; }
 extern "C" {
 
 const char* ig_last_error(void) { return t_err.c_str(); }
-int ig_abi_version(void) { return 1; }
+int ig_abi_version(void) { return 2; }
 int ig_device_count(void) {
   int n = 0;
   if (cudaGetDeviceCount(&n) != cudaSuccess) {

@@ -23,16 +23,32 @@ from ion_gym_gb300.physics.solver3d import (SolveNotConverged, stencil_code,
 
 
 # Method of the FP32 correction solve: method 1 = flexible CG preconditioned
-# by one multigrid cycle, cg_iters iterations per FP64 refinement; method 0 =
-# defect correction with `vcycles` cycles per refinement.  Cycle shape:
+# by one multigrid cycle, cg_iters iterations per refinement step; method 0
+# = defect correction with `vcycles` cycles per step.  Cycle shape:
 # nu1/nu2 red-black smoothing pairs before/after the coarse correction,
-# gamma 1 (V) or 2 (W), smoother relaxation factor.
-# Defaults from a sweep on the GPU with the tail stopping rule: (3, 3) pairs
-# and 3 CG iterations per refinement step beat (2, 2, 4) by 5-8 % on the ring
-# stack, the quadrupole, planar boards and a random deck alike; W-cycles lose
-# on single-problem grids (latency-bound coarse levels).
-CYCLE = {"nu1": 3, "nu2": 3, "vcycles": 2, "gamma": 1, "smooth_omega": 1.0,
-         "method": 1, "cg_iters": 3}
+# gamma 1 (V) or 2 (W; gamma_levels limits the second coarse visit to the
+# finest levels, 0 = all), smoother relaxation factor.
+#
+# The default depends on the batch (from GPU sweeps with the tail stopping
+# rule): a session of one to three problems runs V(3,3) with 3 CG
+# iterations per step -- its coarse launches are small and latency-bound,
+# so a second coarse visit only costs (quadrupole 141 against 98-114
+# solves/s with W) --; a batch of four or more runs (2,2) pairs, 3 CG
+# iterations and a W-cycle at the top level only, whose better coarse
+# correction saves refinement steps once the coarse launches carry the
+# whole batch (8 ring-stack bases 131 -> 174 solves/s, 25 board bases
+# 651 -> 682).
+CYCLE_SINGLE = {"nu1": 3, "nu2": 3, "vcycles": 2, "gamma": 1, "gamma_levels": 0,
+                "smooth_omega": 1.0, "method": 1, "cg_iters": 3}
+CYCLE_BATCH = {"nu1": 2, "nu2": 2, "vcycles": 2, "gamma": 2, "gamma_levels": 1,
+               "smooth_omega": 1.0, "method": 1, "cg_iters": 3}
+BATCH_MIN = 4
+CYCLE = CYCLE_SINGLE   # the single-problem cycle (kept under its old name)
+
+
+def cycle_for(max_problems):
+    """The default cycle of a session holding max_problems problems."""
+    return dict(CYCLE_BATCH if int(max_problems) >= BATCH_MIN else CYCLE_SINGLE)
 
 
 def session_bytes(shape, max_problems):
@@ -48,20 +64,25 @@ class MixedSession:
     sessions of different geometries, driven from different host threads,
     run concurrently on the device."""
 
-    def __init__(self, metal, max_problems, stencil="ghost_linear",
-                 nu1=CYCLE["nu1"], nu2=CYCLE["nu2"],
-                 vcycles=CYCLE["vcycles"], gamma=CYCLE["gamma"],
-                 smooth_omega=CYCLE["smooth_omega"], method=CYCLE["method"],
-                 cg_iters=CYCLE["cg_iters"]):
+    def __init__(self, metal, max_problems, stencil="ghost_linear", **cycle):
+        """cycle: overrides of the batch-size default (`cycle_for`): nu1,
+        nu2, vcycles, gamma, gamma_levels, smooth_omega, method,
+        cg_iters."""
         metal = np.asarray(metal, bool)
         self.shape = metal.shape
         self.max_problems = int(max_problems)
+        unknown = set(cycle) - set(CYCLE_SINGLE)
+        if unknown:
+            raise TypeError(f"MixedSession: unknown cycle settings {sorted(unknown)}")
+        self.cycle = {**cycle_for(self.max_problems), **cycle}
+        c = self.cycle
         self.nbytes = session_bytes(self.shape, self.max_problems)
         self._h = ctypes.c_void_p(None)
         st = _lib.lib().ig_mixed_open_ex(
             ptr(as_mask(metal)), *self.shape, self.max_problems,
-            stencil_code(stencil), int(nu1), int(nu2), int(vcycles),
-            int(gamma), float(smooth_omega), int(method), int(cg_iters),
+            stencil_code(stencil), int(c["nu1"]), int(c["nu2"]),
+            int(c["vcycles"]), int(c["gamma"]), int(c["gamma_levels"]),
+            float(c["smooth_omega"]), int(c["method"]), int(c["cg_iters"]),
             ctypes.byref(self._h))
         _lib.check(st, "MixedSession")
 
@@ -224,7 +245,8 @@ def solve_bases_mixed(masks, v_basis=1e4, accuracy=1e-9,
     fit) on one resident session.  on_batch(done, total, indices), when
     given, is called before each batch (and may raise to stop).  With
     return_stats, also {"steps": the largest refinement-step count of any
-    batch, "batches": n}.  cycle: overrides of CYCLE."""
+    batch, "batches": n}.  cycle: overrides of the batch-size default
+    cycle (`cycle_for`)."""
     metal = _union(masks)
     items = [(i, np.asarray(m, bool)) for i, m in sorted(masks.items())
              if only is None or i in only]
@@ -235,7 +257,7 @@ def solve_bases_mixed(masks, v_basis=1e4, accuracy=1e-9,
     out = {}
     steps = 0
     nb = 0
-    with MixedSession(metal, B, stencil=stencil, **{**CYCLE, **cycle}) as s:
+    with MixedSession(metal, B, stencil=stencil, **cycle) as s:
         for q in range(0, len(items), B):
             part = items[q:q + B]
             if on_batch is not None:

@@ -145,7 +145,11 @@ def solve_code_key(precision=None):
     """The key of the solve-path code of this installation for the basis
     door's precision (None: the door's default, multigrid3d.BASIS_PRECISION)."""
     from ion_gym_gb300.physics import multigrid3d
-    from ion_gym_gb300.physics.mixed import CYCLE
+    from ion_gym_gb300.physics.mixed import CYCLE_SINGLE, CYCLE_BATCH, BATCH_MIN
     p = multigrid3d.basis_precision(precision)
-    cyc = tuple(sorted(CYCLE.items())) if p == "mixed" else ()
+    cyc = ()
+    if p == "mixed":
+        cyc = tuple(sorted({**{f"single_{k}": v for k, v in CYCLE_SINGLE.items()},
+                            **{f"batch_{k}": v for k, v in CYCLE_BATCH.items()},
+                            "batch_min": BATCH_MIN}.items()))
     return _key(p, cyc)

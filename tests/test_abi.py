@@ -40,7 +40,7 @@ def test_ctypes_table_matches_header():
 def test_loads_without_a_device():
     from ion_gym_gb300 import _lib
     L = _lib.lib()
-    assert L.ig_abi_version() == 1
+    assert L.ig_abi_version() == 2
     assert L.ig_device_count() >= 0
     L.ig_request_stop()
     assert L.ig_stop_requested() == 1
