@@ -569,18 +569,22 @@ def run_rings(a):
 def run_uneven(a):
     """Uneven batch (BASELINE config 4): 64 seeded geometries, cubic sides
     from {33,65,97,129,193,257}, 2-16 random electrodes at U(-100,100) V,
-    each solved to 1e-9 of its span by the mixed path; the geometries run
-    concurrently (`workers` at a time, largest grids first; each worker
-    keeps one session per grid shape, rebound to every new deck of that
-    shape, so a deck costs its mask upload and coarsening but no session
-    build).  Each deck arrives as host buffers (metal
-    mask, Dirichlet values) in pinned memory, as a serving caller hands them
-    over, and its potential is returned into a pinned host buffer: every
-    upload, session build and download is inside the timed region.  One
-    step = the whole batch of 64.  `roofline`: the algorithmic bytes of
-    every refinement step of every deck over the batch's time."""
+    each solved to 1e-9 of its own span by the mixed path.  One step = the
+    whole batch of 64; every upload, mask build, solve and download is
+    inside the timed region.
+
+    --uneven-mode shape (default): the decks of each grid shape run as one
+    batch -- a session with one metal per problem, so every launch of a
+    refinement step covers all decks of the shape -- the six shapes
+    concurrently, largest first; each shape's masks and values are handed
+    over as one pinned stack and its potentials come back into one.
+    --uneven-mode deck: each deck on its own (12 workers, a session per
+    grid shape and worker rebound to every new deck), pinned buffers per
+    deck.  `resident`: the same solves with the sessions built and the
+    values already on the device -- the kernels alone."""
     import concurrent.futures as cf
     import ctypes
+    import threading
     import torch
     from ion_gym_gb300 import _lib
     from ion_gym_gb300.workloads import random_deck
@@ -590,122 +594,166 @@ def run_uneven(a):
     rng = np.random.default_rng(2026)
     sides = rng.choice([33, 65, 97, 129, 193, 257], 64)
     nel = rng.integers(2, 17, 64)
+    nodes = sum(int(sd) ** 3 for sd in sides)
+    peak = _peak()
 
-    def pinned(x):
-        t = torch.empty(x.shape, dtype=getattr(torch, str(x.dtype))).pin_memory()
-        h = t.numpy()
-        h[...] = x
-        return h
+    def pinned_like(shape, dtype):
+        return torch.empty(shape, dtype=dtype).pin_memory().numpy()
 
-    decks = []
+    raw = []
     for q, (sd, k) in enumerate(zip(sides, nel)):
         fixed, val = random_deck(1000 + q, int(sd), int(k))
-        span = max(float(val.max() - val.min()), 1.0)
-        decks.append((pinned(fixed), pinned(val), pinned(np.zeros(val.shape)), span))
+        raw.append((fixed, val, max(float(val.max() - val.min()), 1.0)))
 
-    # each worker keeps one session per grid shape and rebinds it to the
-    # next deck of that shape (the new metal's masks on every level; the
-    # buffers and captured graphs stay): a new geometry costs no session
-    # build once its shape has been seen
-    import threading
-    tl = threading.local()
-    opened = []
-    olock = threading.Lock()
+    if a.uneven_mode == "deck":
+        order = sorted(range(64), key=lambda q: -int(sides[q]) ** 3)
+        items = []
+        for q in range(64):
+            f, v, sp = raw[q]
+            fh = pinned_like(f.shape, torch.bool)
+            fh[...] = f
+            vh = pinned_like(v.shape, torch.float64)
+            vh[...] = v
+            items.append((fh, vh, pinned_like(v.shape, torch.float64), sp))
+        workers = a.workers if a.workers > 4 else 12
+        tl = threading.local()
+        opened = []
+        olock = threading.Lock()
 
-    def solve(d):
-        fixed, val, out, span = d
-        cache = getattr(tl, "sessions", None)
-        if cache is None:
-            cache = tl.sessions = {}
-        s = cache.get(fixed.shape)
-        if s is None:
-            s = cache[fixed.shape] = MixedSession(fixed, 1)
-            with olock:
-                opened.append(s)
-        else:
-            s.rebind(fixed)
-        s.solve_values(val, 1e-9, out=out, span=span)
-        return s.last_steps, s.last_steps * s.step_bytes(1)
+        def solve(q):
+            fixed, val, out, span = items[q]
+            cache = getattr(tl, "sessions", None)
+            if cache is None:
+                cache = tl.sessions = {}
+            s = cache.get(fixed.shape)
+            if s is None:
+                s = cache[fixed.shape] = MixedSession(fixed, 1)
+                with olock:
+                    opened.append(s)
+            else:
+                s.rebind(fixed)
+            s.solve_values(val, 1e-9, out=out, span=span)
+            return [s.last_steps], s.last_steps * s.step_bytes(1)
+        units = order
+    else:
+        groups = {}
+        for q in range(64):
+            groups.setdefault(int(sides[q]), []).append(q)
+        order = sorted(groups, key=lambda sd: -sd)
+        items = {}
+        for sd in order:
+            qs = groups[sd]
+            shape = (len(qs), sd, sd, sd)
+            fh = pinned_like(shape, torch.bool)
+            vh = pinned_like(shape, torch.float64)
+            for b, q in enumerate(qs):
+                fh[b] = raw[q][0]
+                vh[b] = raw[q][1]
+            spans = np.array([raw[q][2] for q in qs])
+            items[sd] = (fh, vh, pinned_like(shape, torch.float64), spans)
+        workers = len(order)
+        sessions = {}
 
-    # largest geometries first (longest-processing-time order), so the
-    # small ones fill the device while the last large ones finish
-    order = sorted(range(len(decks)), key=lambda q: -int(sides[q]) ** 3)
-    workers = a.workers if a.workers > 4 else 12
+        def solve(sd):
+            fixed, val, out, spans = items[sd]
+            s = sessions.get(sd)
+            if s is None:
+                s = sessions[sd] = MixedSession(fixed)
+            else:
+                s.rebind(fixed)
+            s.solve_values(val, 1e-9, out=out, span=spans)
+            return [s.last_steps] * len(spans), s.last_steps * s.step_bytes(len(spans))
+        opened = sessions
+        units = order
+
     steps = []
     with cf.ThreadPoolExecutor(workers) as ex:
         for _ in range(max(a.warmup, 1)):
-            list(ex.map(solve, [decks[q] for q in order]))
+            list(ex.map(solve, units))
         torch.cuda.synchronize()
         clocks = Clocks(0)
         launches0 = L.ig_launch_count() + _mixed_launches(L)
         clocks.start()
         t0 = time.perf_counter()
         for _ in range(a.steps):
-            steps = list(ex.map(solve, [decks[q] for q in order]))
+            steps = list(ex.map(solve, units))
         torch.cuda.synchronize()
         el = time.perf_counter() - t0
         ck = clocks.stop()
         launches = L.ig_launch_count() + _mixed_launches(L) - launches0
-    for s_ in opened:
-        s_.close()
-    nodes = sum(int(sd) ** 3 for sd in sides)
-    nsteps = [st for st, _ in steps]
+    nsteps = [x for st, _ in steps for x in st]
     byts = sum(b for _, b in steps)
     achieved = byts * a.steps / el / 1e9
-    peak = _peak()
-    # the kernels alone: every deck's session built beforehand and its
-    # values resident on the device, the 64 solves run by the same 12
-    # workers -- what any scheduling of these kernels (a persistent
-    # work-queue launch included) has to improve on
+
+    # the kernels alone: the sessions built, the values on the device
     resident = None
     try:
-        sess = [MixedSession(decks[q][0], 1) for q in order]
-        vdev = [torch.from_numpy(np.asarray(decks[q][1])).cuda() for q in order]
+        if a.uneven_mode == "deck":
+            for s_ in (opened if isinstance(opened, list) else []):
+                s_.close()
+            res = [(MixedSession(raw[q][0], 1), [q]) for q in order]
+        else:
+            res = [(opened[sd], groups[sd]) for sd in order]
+        vdev = [torch.from_numpy(np.stack([raw[q][1] for q in qs])).cuda()
+                for _, qs in res]
         odev = [torch.empty_like(v) for v in vdev]
+        accs = [np.ascontiguousarray(1e-9 * np.array([raw[q][2] for q in qs]))
+                for _, qs in res]
 
         def solve_res(k):
-            s = sess[k]
+            s, qs = res[k]
             st_ = ctypes.c_int(0)
-            dm = np.zeros(1)
-            rc = L.ig_mixed_solve_values(s._h, ctypes.c_void_p(vdev[k].data_ptr()), 1,
-                                         1e-9 * decks[order[k]][3], 40,
-                                         ctypes.c_void_p(odev[k].data_ptr()),
-                                         ctypes.byref(st_), dm.ctypes.data_as(ctypes.c_void_p))
+            dm = np.zeros(len(qs))
+            rc = L.ig_mixed_solve_values_acc(
+                s._h, ctypes.c_void_p(vdev[k].data_ptr()), len(qs),
+                accs[k].ctypes.data_as(ctypes.c_void_p), 40,
+                ctypes.c_void_p(odev[k].data_ptr()), ctypes.byref(st_),
+                dm.ctypes.data_as(ctypes.c_void_p))
             _lib.check(rc, "uneven resident solve")
-            return st_.value * s.step_bytes(1)
+            return st_.value * s.step_bytes(len(qs))
 
         with cf.ThreadPoolExecutor(workers) as ex:
-            list(ex.map(solve_res, range(len(sess))))
+            list(ex.map(solve_res, range(len(res))))
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             rb = 0.0
             for _ in range(a.steps):
-                rb += sum(ex.map(solve_res, range(len(sess))))
+                rb += sum(ex.map(solve_res, range(len(res))))
             torch.cuda.synchronize()
             el_r = time.perf_counter() - t0
         resident = {"value": 64 * a.steps / el_r, "unit": "solves/s",
                     "node_solves_s": nodes * a.steps / el_r,
                     "achieved_gbs": rb / el_r / 1e9,
                     "frac": rb / el_r / 1e9 / peak if peak else None,
-                    "what": "sessions resident, values on the device: the "
+                    "what": "sessions built, values on the device: the "
                             "kernels of the 64 solves alone"}
-        for s_ in sess:
+        for s_, _ in res:
             s_.close()
-        del sess, vdev, odev
-    except Exception as ex_:      # too little device memory for 64 sessions
+        del vdev, odev
+    except Exception as ex_:      # too little device memory
         resident = {"unavailable": str(ex_)[:200]}
+    if a.uneven_mode != "deck":
+        for s_ in opened.values():
+            s_.close()
+
+    mode = ("decks of one grid shape as one batch (one metal per problem, "
+            "every launch covering all of them), the six shapes concurrently"
+            if a.uneven_mode != "deck" else
+            "each deck on its own: 12 workers, a session per grid shape and "
+            "worker rebound to each new deck")
     line = {
         "metric": METRIC, "value": 64 * a.steps / el, "unit": "solves/s",
         "n_gpus": 1, "steps": a.steps, "warmup": max(a.warmup, 1),
         "ms_per_step": 1e3 * el / a.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f32 sweeps + f64 refinement",
+        "dtype": "f32 sweeps + f64 refinement (fixed-point potential)",
         "data": "synthetic (64 seeded random decks)",
         "config": {"workload": "uneven_batch_64_mixed", "sides":
                    [int(sd) for sd in sides], "nodes": nodes,
-                   "accuracy_of_span": 1e-9, "concurrent_sessions": workers,
+                   "accuracy_of_span": 1e-9, "mode": mode,
                    "order": "largest grid first",
-                   "host_buffers": "pinned (mask, values in; potential out)",
+                   "host_buffers": "pinned (mask, values in; potential out)"
+                   + (", one stack per grid shape" if a.uneven_mode != "deck" else ""),
                    "l2": "inputs larger than L2 (the batch holds GBs)"},
         "refinement_steps": {"min": int(min(nsteps)), "max": int(max(nsteps))},
         "node_solves_s": nodes * a.steps / el,
@@ -718,8 +766,8 @@ def run_uneven(a):
                      "traffic": None,
                      "kernel": "the whole batch: algorithmic bytes of every "
                                "refinement step of every deck (all kernels, "
-                               "all levels) over the batch's time, session "
-                               "builds and host copies included in the time",
+                               "all levels) over the batch's time, uploads, "
+                               "mask builds and downloads included in the time",
                      "bytes_per_step": byts},
         "clocks": ck}
     if not a.no_cpu:
@@ -730,9 +778,9 @@ def run_uneven(a):
         small = sorted(range(64), key=lambda q: int(sides[q]))[:6]
         t = time.perf_counter()
         for q in small:
-            fx, v, _, span = decks[q]
-            port.solve3d_vmg(np.asarray(fx, bool), np.asarray(v), tol=1e-9 * span,
-                             max_cycles=200, accept_stagnation=True)
+            fx, v, span = raw[q]
+            port.solve3d_vmg(fx, v, tol=1e-9 * span, max_cycles=200,
+                             accept_stagnation=True)
         tc = time.perf_counter() - t
         snodes = sum(int(sides[q]) ** 3 for q in small)
         rate = snodes / tc                       # node-solves/s
@@ -1082,6 +1130,8 @@ def main():
     ap.add_argument("--ring-frac", type=float, default=0.2,
                     help="serve: fraction of ring-stack (config 3) decks")
     ap.add_argument("--workers", type=int, default=4)
+    ap.add_argument("--uneven-mode", default="shape", choices=["shape", "deck"],
+                    help="uneven: decks of one grid shape as one batch, or one by one")
     a = ap.parse_args()
     if a.impl == "reference":
         run_reference(a)

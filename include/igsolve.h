@@ -186,19 +186,37 @@ int ig_mixed_open_ex(const uint8_t *metal, long nx, long ny, long nz,
                      int vcycles, int gamma, int gamma_levels,
                      double smooth_omega, int method, int cg_iters,
                      void **handle);
+/* A session with one metal per problem (no reference counterpart): the
+ * n_problems stacked (nx, ny, nz) uint8 masks in `metals`, problem p
+ * solved on metal p by ig_mixed_solve_values (problems 0..P-1 of a call on
+ * metals 0..P-1), so decks of one grid shape with different electrodes run
+ * as one batch: every launch of a refinement step covers all of them.
+ * ig_mixed_rebind then takes n_problems stacked masks; ig_mixed_solve_bases
+ * is refused (IG_BAD_ARG).  ig_mixed_bytes_multi: its device bytes. */
+int ig_mixed_open_multi(const uint8_t *metals, int n_problems, long nx, long ny,
+                        long nz, int stencil, int nu1, int nu2, int vcycles,
+                        int gamma, int gamma_levels, double smooth_omega,
+                        int method, int cg_iters, void **handle);
+long ig_mixed_bytes_multi(long nx, long ny, long nz, int n_problems);
 int ig_mixed_solve_bases(void *handle, const uint8_t *masks, int n_bases,
                          double v_basis, double acc, int max_steps,
                          double *phi_out, int *steps_out, double *dmax_out);
 int ig_mixed_solve_values(void *handle, const double *vals, int n_problems,
                           double acc, int max_steps, double *phi_out,
                           int *steps_out, double *dmax_out);
+/* ig_mixed_solve_values with one absolute accuracy per problem (acc[p]
+ * volts for problem p; no reference counterpart). */
+int ig_mixed_solve_values_acc(void *handle, const double *vals, int n_problems,
+                              const double *acc, int max_steps, double *phi_out,
+                              int *steps_out, double *dmax_out);
 void ig_mixed_close(void *handle);
 /* Gives a session another geometry of its shape (no reference
  * counterpart): the new metal union's masks replace the old ones on every
  * level; the buffers, the tuned smoother shape and the captured graphs stay,
  * so a solve on the rebound session costs no session build.  The results
  * are those of a session opened on the new metal.  IG_BAD_ARG when the
- * shape differs. */
+ * shape differs.  A session with one metal per problem takes its
+ * n_problems masks stacked. */
 int ig_mixed_rebind(void *handle, const uint8_t *metal, long nx, long ny,
                     long nz);
 /* Times `pairs` red-black pairs of the session's fine-level FP32

@@ -94,6 +94,10 @@ SIGNATURES = {
     "ig_mixed_time_gs": (_i, [_p, _i, _i, _pd, _pd]),
     "ig_mixed_step_bytes": (_i, [_p, _i, _pd]),
     "ig_mixed_rebind": (_i, [_p, _p, _l, _l, _l]),
+    "ig_mixed_open_multi": (_i, [_p, _i, _l, _l, _l, _i, _i, _i, _i, _i, _i,
+                                 _d, _i, _i, ctypes.POINTER(ctypes.c_void_p)]),
+    "ig_mixed_bytes_multi": (_l, [_l, _l, _l, _i]),
+    "ig_mixed_solve_values_acc": (_i, [_p, _p, _i, _p, _i, _p, _pi, _p]),
     "ig_mixed_check_fused": (_i, [_p, _i, ctypes.POINTER(ctypes.c_longlong)]),
     "ig_cascadic_relres_noalloc": (_i, [_p, _p, _l, _l, _l, _d, _l, _i, _i,
                                         _d, _p, _i, _i, _p, _pl, _pd, _pl,

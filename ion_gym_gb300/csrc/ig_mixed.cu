@@ -64,6 +64,9 @@ struct SGeo {
                             // up to a multiple of 4 (16-byte aligned rows)
   uint32_t csz;             // nx * ny * H (one colour array)
   uint32_t n;               // nx * ny * nz (natural)
+  // per-problem strides of the metal masks (bytes): the split masks of the
+  // level and the natural fine mask; 0 when every problem shares one metal
+  uint32_t msplit = 0, mnat = 0;
   FastDiv dH, dny, dnz, dH4, dH8;  // dH8: pairs of float4 groups per row
 };
 
@@ -234,6 +237,7 @@ template <int NG, bool FLAT>
 __global__ void k_gs4(float* __restrict__ e, const float* __restrict__ g,
                       const uint8_t* __restrict__ mask, SGeo G, int c, float omega,
                       size_t pstride) {
+  mask += (size_t)blockIdx.y * G.msplit;
   const uint32_t nq = G.csz >> 2;
   float* eb = e + blockIdx.y * pstride;
   float* own = eb + (size_t)c * G.csz;
@@ -256,6 +260,7 @@ template <bool FLAT>
 __global__ void k_gs8(float* __restrict__ e, const float* __restrict__ g,
                       const uint8_t* __restrict__ mask, SGeo G, int c, float omega,
                       size_t pstride) {
+  mask += (size_t)blockIdx.y * G.msplit;
   const uint32_t H4 = (uint32_t)(G.H >> 2);
   const uint32_t npair = (uint32_t)G.nx * G.ny * G.dH8.d;
   const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -296,6 +301,7 @@ __device__ __forceinline__ float4 zero_start_e0(const float* gp, const uint8_t* 
 __global__ void __launch_bounds__(kT)
 k_gs_zero_pair(float* __restrict__ e, const float* __restrict__ g,
                const uint8_t* __restrict__ mask, SGeo G, size_t pstride) {
+  mask += (size_t)blockIdx.y * G.msplit;
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= (G.csz >> 2)) return;
   const uint32_t ij = fdivu(t, G.dH4);
@@ -411,6 +417,7 @@ template <int S, bool ZERO, int C1, int TY, int TMG, int MINB>
 __global__ void __launch_bounds__(TbShape<S, TY, TMG>::NT, MINB)
 k_gs_tb(const float* __restrict__ ein, float* __restrict__ eout, const float* __restrict__ g,
         const uint8_t* __restrict__ mask, SGeo G, size_t pstride) {
+  mask += (size_t)blockIdx.y * G.msplit;
   using Sh = TbShape<S, TY, TMG>;
   constexpr int R = Sh::R, GR = Sh::GR, NT = Sh::NT;
   extern __shared__ float4 tb_sm[];  // [stage 0..S-1][parity][NT]; stage 0 = input
@@ -594,6 +601,7 @@ __global__ void __launch_bounds__(kT)
 k_resid0(const float* __restrict__ e, const float* __restrict__ g,
          const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ r,
          size_t pstride) {
+  mask += (size_t)blockIdx.y * G.msplit;
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= G.csz) return;
   const uint32_t ij = fdivu(t, G.dH);
@@ -617,6 +625,7 @@ __global__ void __launch_bounds__(kT)
 k_resid0_4(const float* __restrict__ e, const float* __restrict__ g,
            const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ r,
            size_t pstride) {
+  mask += (size_t)blockIdx.y * G.msplit;
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= (G.csz >> 2)) return;
   const uint32_t ij = fdivu(t, G.dH4);
@@ -785,6 +794,7 @@ __global__ void __launch_bounds__(kT)
 k_resid(const float* __restrict__ e, const float* __restrict__ g,
         const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ r,
         size_t pstride, size_t rstride) {
+  mask += (size_t)blockIdx.y * G.msplit;
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= G.n) return;
   const uint32_t ij = fdivu(t, G.dnz);
@@ -871,6 +881,7 @@ __global__ void __launch_bounds__(kT)
 k_prolong_add4_gather(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
                const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
                size_t fstride) {
+  maskf += (size_t)blockIdx.y * F.msplit;
   const int c = blockIdx.z;  // gridDim.z = 1: colour 0 only
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= (F.csz >> 2)) return;
@@ -934,6 +945,7 @@ __global__ void __launch_bounds__(kT)
 k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
                const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
                size_t fstride) {
+  maskf += (size_t)blockIdx.y * F.msplit;
   const int c = blockIdx.z;  // gridDim.z = 1: colour 0 only
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= (F.csz >> 2)) return;
@@ -1008,6 +1020,7 @@ __global__ void __launch_bounds__(kBottomThreads)
 k_bottom(float* __restrict__ e, const float* __restrict__ g,
          const uint8_t* __restrict__ mask, SGeo G, float omega, int pairs,
          size_t pstride) {
+  mask += (size_t)blockIdx.x * G.msplit;
   __shared__ float se[kBottomMax];
   __shared__ float sg[kBottomMax];
   __shared__ uint8_t sm[kBottomMax];
@@ -1151,6 +1164,7 @@ __global__ void __launch_bounds__(kT)
 k_resid64(const long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
           SGeo G, float* __restrict__ g, const int* __restrict__ fexp, float nscale,
           size_t nstride, size_t pstride) {
+  fixed += (size_t)blockIdx.y * G.mnat;
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= G.n) return;
   const uint32_t ij = fdivu(t, G.dnz);
@@ -1206,6 +1220,7 @@ k_update64_8(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
              const float* __restrict__ e, SGeo G, unsigned long long* dmax,
              const int* __restrict__ fexp, size_t nstride, size_t pstride,
              const float* __restrict__ p = nullptr, const double* __restrict__ scal = nullptr) {
+  fixed += (size_t)blockIdx.y * G.mnat;
   // The block's groups cover one contiguous natural range [n_lo, n_hi) (a
   // row's valid groups are consecutive and the next row starts where it
   // ends; groups past a row's end cover nothing), at most 8 kT nodes: the
@@ -1284,9 +1299,10 @@ __global__ void k_init_basis(long long* __restrict__ phi, const uint8_t* __restr
 
 __global__ void k_init_vals(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
                             const double* __restrict__ val, uint32_t n, size_t nstride,
-                            const int* __restrict__ fexp) {
+                            const int* __restrict__ fexp, size_t fstride) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= n) return;
+  fixed += blockIdx.y * fstride;
   const double v = val[blockIdx.y * nstride + t];
   phi[blockIdx.y * nstride + t] =
       fixed[t] ? __double2ll_rn(v * pow2d(56 - fexp[blockIdx.y])) : 0LL;
@@ -1297,7 +1313,8 @@ __global__ void k_init_vals(long long* __restrict__ phi, const uint8_t* __restri
 // range check refuses them).
 __global__ void __launch_bounds__(kT)
 k_absmax_vals(const double* __restrict__ val, const uint8_t* __restrict__ fixed, uint32_t n,
-              size_t nstride, unsigned long long* out) {
+              size_t nstride, unsigned long long* out, size_t fstride) {
+  fixed += blockIdx.y * fstride;
   unsigned long long key = 0;
   for (uint32_t t = blockIdx.x * kT + threadIdx.x; t < n; t += gridDim.x * kT) {
     if (!fixed[t]) continue;
@@ -1317,9 +1334,10 @@ k_absmax_vals(const double* __restrict__ val, const uint8_t* __restrict__ fixed,
 __global__ void k_fixed_out(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
                             const double* __restrict__ vals, const uint8_t* __restrict__ masks,
                             double v, uint32_t n, size_t nstride,
-                            const int* __restrict__ fexp) {
+                            const int* __restrict__ fexp, size_t fstride) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= n) return;
+  fixed += blockIdx.y * fstride;
   const size_t o = blockIdx.y * nstride + t;
   double r;
   if (fixed[t])
@@ -1386,6 +1404,7 @@ __global__ void __launch_bounds__(kT)
 k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
             const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ q,
             double* __restrict__ part, size_t pstride) {
+  mask += (size_t)blockIdx.y * G.msplit;
   __shared__ double sh[kT / 32];
   const int c = blockIdx.z;
   const uint32_t nq = G.csz >> 2;
@@ -1440,6 +1459,7 @@ k_cg_matvec_dir(const float* __restrict__ z, const float* __restrict__ po,
                 float* __restrict__ pn, const double* __restrict__ scal,
                 const float* __restrict__ g, const uint8_t* __restrict__ mask, SGeo G,
                 float* __restrict__ q, double* __restrict__ part, size_t pstride) {
+  mask += (size_t)blockIdx.y * G.msplit;
   __shared__ double sh[kT / 32];
   const int c = blockIdx.z;
   const uint32_t nq = G.csz >> 2;
@@ -1623,12 +1643,13 @@ bool is_bottom(const Dims& d) {
 }
 
 // Device bytes a session holds (for admission control by HBM footprint).
-size_t session_bytes(Dims fine, int bmax) {
-  size_t b = fine.n() * (1 + 8 * (size_t)bmax + (size_t)bmax);  // mask, phi, masks/values staging
+size_t session_bytes(Dims fine, int bmax, int nmetal = 1) {
+  // fine masks, phi, masks/values staging
+  size_t b = fine.n() * ((size_t)nmetal + 8 * (size_t)bmax + (size_t)bmax);
   Dims d = fine;
   while (true) {
     const size_t csz = (size_t)d.nx * d.ny * (size_t)((((d.nz + 1) / 2) + 3) & ~3L);
-    b += d.n() + 2 * csz + 2 * (2 * csz * 4 * (size_t)bmax);
+    b += (d.n() + 2 * csz) * (size_t)nmetal + 2 * (2 * csz * 4 * (size_t)bmax);
     // level 0: the flexible CG's correction, two direction buffers and L p
     if (d.n() == fine.n()) b += 4 * (2 * csz * 4 * (size_t)bmax);
     if (is_bottom(d)) break;
@@ -1655,6 +1676,7 @@ struct Session {
   Dims d;
   int bmax = 1;
   int B = 1;  // problems of the current call
+  int nmetal = 1;  // 1: one metal for every problem; bmax: problem p on metal p
   std::vector<MLevel> lv;
   Buf<long long> phi;   // refined potentials, fixed point (units 2^(fexp[b] - 56))
   Buf<int> fexp;        // per problem: the unit exponent E_b
@@ -1727,39 +1749,49 @@ struct Session {
   // buffers.  Nothing else of a session depends on the metal, so a session
   // can take another geometry of its shape (ig_mixed_rebind) and keep its
   // buffers, tuned smoother shape and captured graphs.
+  // metal: nmetal stacked (nx, ny, nz) masks (nmetal = 1: one metal shared
+  // by every problem; nmetal = bmax: problem p on metal p).
   void load_metal(const uint8_t* metal) {
     const size_t n = d.n();
-    MK(cudaMemcpyAsync(fixed.p, metal, n, cudaMemcpyDefault, s));
+    MK(cudaMemcpyAsync(fixed.p, metal, n * nmetal, cudaMemcpyDefault, s));
     Buf<uint8_t> inj;
     if (lv.size() > 1) inj.alloc(lv[1].G.n, s);
-    for (size_t l = 0; l < lv.size(); l++) {
-      MLevel& L = lv[l];
-      if (l == 0) {
-        MK(cudaMemcpyAsync(L.nat.p, fixed.p, n, cudaMemcpyDeviceToDevice, s));
-      } else {
-        const MLevel& F = lv[l - 1];
-        k_coarsen_inject<<<nblk(L.G.n), kT, 0, s>>>(F.nat.p, F.G, inj.p, L.G);
-        MK(cudaGetLastError());
-        k_coarsen_rescue<<<nblk(L.G.n), kT, 0, s>>>(F.nat.p, F.G, inj.p, L.nat.p, L.G);
+    for (int q = 0; q < nmetal; q++)
+      for (size_t l = 0; l < lv.size(); l++) {
+        MLevel& L = lv[l];
+        uint8_t* nat = L.nat.p + (size_t)q * L.G.n;
+        if (l == 0) {
+          MK(cudaMemcpyAsync(nat, fixed.p + (size_t)q * n, n, cudaMemcpyDeviceToDevice, s));
+        } else {
+          const MLevel& F = lv[l - 1];
+          const uint8_t* fnat = F.nat.p + (size_t)q * F.G.n;
+          k_coarsen_inject<<<nblk(L.G.n), kT, 0, s>>>(fnat, F.G, inj.p, L.G);
+          MK(cudaGetLastError());
+          k_coarsen_rescue<<<nblk(L.G.n), kT, 0, s>>>(fnat, F.G, inj.p, nat, L.G);
+          MK(cudaGetLastError());
+        }
+        uint8_t* mk = L.mask.p + (size_t)q * 2 * L.G.csz;
+        MK(cudaMemsetAsync(mk, 1, 2 * (size_t)L.G.csz, s));  // unused slots: metal
+        k_split_mask<<<nblk(L.G.n), kT, 0, s>>>(nat, L.G, mk);
         MK(cudaGetLastError());
       }
-      MK(cudaMemsetAsync(L.mask.p, 1, 2 * (size_t)L.G.csz, s));  // unused slots: metal
-      k_split_mask<<<nblk(L.G.n), kT, 0, s>>>(L.nat.p, L.G, L.mask.p);
-      MK(cudaGetLastError());
-    }
-    g_mixed_launches.fetch_add(3L * (long)lv.size());
+    g_mixed_launches.fetch_add(3L * (long)lv.size() * nmetal);
   }
 
   void build(const uint8_t* metal) {
     const size_t n = d.n();
-    fixed.alloc(n, s);
+    fixed.alloc(n * nmetal, s);
     Dims c = d;
     while (true) {
       MLevel L;
       L.d = c;
       L.G = sgeo(c);
-      L.nat.alloc(c.n(), s);
-      L.mask.alloc(2 * (size_t)L.G.csz, s);
+      if (nmetal > 1) {
+        L.G.msplit = 2 * L.G.csz;
+        L.G.mnat = (uint32_t)n;  // the natural mask is read on level 0 only
+      }
+      L.nat.alloc(c.n() * nmetal, s);
+      L.mask.alloc(2 * (size_t)L.G.csz * nmetal, s);
       L.pstride = 2 * (size_t)L.G.csz;
       L.rstride = L.G.n;
       L.e.alloc(L.pstride * bmax, s);
@@ -2181,7 +2213,7 @@ struct MixedResult {
 // first step has no ratio and never stops a problem with a nonzero change.
 constexpr double kRhoSafety = 3.0;
 
-MixedResult run_mixed(Session& M, double acc, int max_steps) {
+MixedResult run_mixed(Session& M, const double* acc, int max_steps) {
   if (M.method == 1) M.cg_init();
   std::vector<unsigned long long> h(M.B);
   std::vector<double> prev(M.B, INFINITY), prev_rho(M.B, 0.0);
@@ -2198,7 +2230,7 @@ MixedResult run_mixed(Session& M, double acc, int max_steps) {
       const double r = std::isfinite(prev[b]) && prev[b] > 0 ? d / prev[b] : 1.0;
       const double rho = std::min(kRhoSafety * std::max(r, prev_rho[b]), 0.95);
       const double tail = d * rho / (1.0 - rho);
-      if (!(tail < acc) && !(d == 0.0)) all = false;
+      if (!(tail < acc[b]) && !(d == 0.0)) all = false;
       prev[b] = d;
       prev_rho[b] = r;
     }
@@ -2243,7 +2275,7 @@ int finish(Session& S, const MixedResult& r, double* phi_out, int* steps_out,
   g_mixed_launches.fetch_add(S.launches_per_step() * r.steps + 1);
   const uint32_t n = (uint32_t)S.d.n();
   k_fixed_out<<<dim3(nblk(n), S.B), kT, 0, S.s>>>(S.phi.p, S.fixed.p, vals, masks, v, n, n,
-                                                  S.fexp.p);
+                                                  S.fexp.p, S.lv[0].G.mnat);
   MK(cudaGetLastError());
   MK(cudaMemcpyAsync(phi_out, S.phi.p, S.d.n() * S.B * 8, cudaMemcpyDefault, S.s));
   MK(cudaStreamSynchronize(S.s));
@@ -2277,10 +2309,15 @@ int ig_mixed_open(const uint8_t* metal, long nx, long ny, long nz,
                           vcycles, 1, 0, 1.0, 1, 3, handle);
 }
 
-int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
-                     int max_problems, int stencil, int nu1, int nu2,
-                     int vcycles, int gamma, int gamma_levels, double smooth_omega,
-                     int method, int cg_iters, void** handle) {
+}  // extern "C"
+
+namespace {
+// Opens a session; nmetal = 1 (one metal, `metal`) or max_problems
+// (`metal` stacks one mask per problem).
+int open_session(const uint8_t* metal, int nmetal, long nx, long ny, long nz,
+                 int max_problems, int stencil, int nu1, int nu2, int vcycles, int gamma,
+                 int gamma_levels, double smooth_omega, int method, int cg_iters,
+                 void** handle) {
   set_last_error("");
   if (!handle || !metal) {
     set_last_error("null argument");
@@ -2307,6 +2344,7 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
     MK(cudaStreamCreateWithFlags(&S->s, cudaStreamNonBlocking));
     S->d = Dims{nx, ny, nz};
     S->bmax = max_problems;
+    S->nmetal = nmetal;
     S->nu1 = std::max(0, nu1);
     S->nu2 = std::max(1, nu2);
     S->vcycles = std::max(1, vcycles);
@@ -2333,6 +2371,34 @@ int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
   *handle = S;
   return IG_OK;
 }
+}  // namespace
+
+extern "C" {
+
+int ig_mixed_open_ex(const uint8_t* metal, long nx, long ny, long nz,
+                     int max_problems, int stencil, int nu1, int nu2,
+                     int vcycles, int gamma, int gamma_levels, double smooth_omega,
+                     int method, int cg_iters, void** handle) {
+  return open_session(metal, 1, nx, ny, nz, max_problems, stencil, nu1, nu2, vcycles, gamma,
+                      gamma_levels, smooth_omega, method, cg_iters, handle);
+}
+
+int ig_mixed_open_multi(const uint8_t* metals, int n_problems, long nx, long ny, long nz,
+                        int stencil, int nu1, int nu2, int vcycles, int gamma,
+                        int gamma_levels, double smooth_omega, int method, int cg_iters,
+                        void** handle) {
+  if (n_problems < 1) {
+    set_last_error("ig_mixed_open_multi: n_problems must be >= 1");
+    return IG_BAD_ARG;
+  }
+  return open_session(metals, n_problems, nx, ny, nz, n_problems, stencil, nu1, nu2, vcycles,
+                      gamma, gamma_levels, smooth_omega, method, cg_iters, handle);
+}
+
+long ig_mixed_bytes_multi(long nx, long ny, long nz, int n_problems) {
+  if (nx < 1 || ny < 1 || nz < 1 || n_problems < 1) return -1;
+  return (long)session_bytes(Dims{nx, ny, nz}, n_problems, n_problems);
+}
 
 void ig_mixed_close(void* handle) { delete static_cast<Session*>(handle); }
 
@@ -2348,7 +2414,7 @@ int ig_mixed_rebind(void* handle, const uint8_t* metal, long nx, long ny, long n
     return IG_BAD_ARG;
   }
   try {
-    S->load_metal(metal);
+    S->load_metal(metal);             // nmetal masks for a per-problem session
     MK(cudaStreamSynchronize(S->s));  // the caller may reuse its mask buffer
   } catch (int code) {
     return code;
@@ -2575,6 +2641,11 @@ int ig_mixed_solve_bases(void* handle, const uint8_t* masks, int n_bases,
     set_last_error("null argument or basis count outside 1..max_problems");
     return IG_BAD_ARG;
   }
+  if (S->nmetal > 1) {
+    set_last_error("ig_mixed_solve_bases: a session with one metal per problem solves "
+                   "values (ig_mixed_solve_values), not the bases of one metal union");
+    return IG_BAD_ARG;
+  }
   try {
     const size_t n = S->d.n();
     S->B = n_bases;
@@ -2588,7 +2659,8 @@ int ig_mixed_solve_bases(void* handle, const uint8_t* masks, int n_bases,
     k_init_basis<<<dim3(nblk((uint32_t)n), n_bases), kT, 0, S->s>>>(S->phi.p, S->stage.p,
                                                                    (uint32_t)n, vfx, n);
     MK(cudaGetLastError());
-    const MixedResult r = run_mixed(*S, acc, max_steps);
+    const std::vector<double> accs(n_bases, acc);
+    const MixedResult r = run_mixed(*S, accs.data(), max_steps);
     return finish(*S, r, phi_out, steps_out, dmax_out, nullptr, S->stage.p, v_basis);
   } catch (int code) {
     return code;
@@ -2598,9 +2670,21 @@ int ig_mixed_solve_bases(void* handle, const uint8_t* masks, int n_bases,
 int ig_mixed_solve_values(void* handle, const double* vals, int n_problems,
                           double acc, int max_steps, double* phi_out,
                           int* steps_out, double* dmax_out) {
+  if (n_problems < 1 || n_problems > 65535) {
+    set_last_error("problem count outside 1..max_problems");
+    return IG_BAD_ARG;
+  }
+  const std::vector<double> accs(n_problems, acc);
+  return ig_mixed_solve_values_acc(handle, vals, n_problems, accs.data(), max_steps, phi_out,
+                                   steps_out, dmax_out);
+}
+
+int ig_mixed_solve_values_acc(void* handle, const double* vals, int n_problems,
+                              const double* acc, int max_steps, double* phi_out,
+                              int* steps_out, double* dmax_out) {
   set_last_error("");
   Session* S = static_cast<Session*>(handle);
-  if (!S || !vals || !phi_out || n_problems < 1 || n_problems > S->bmax) {
+  if (!S || !vals || !phi_out || !acc || n_problems < 1 || n_problems > S->bmax) {
     set_last_error("null argument or problem count outside 1..max_problems");
     return IG_BAD_ARG;
   }
@@ -2611,7 +2695,7 @@ int ig_mixed_solve_values(void* handle, const double* vals, int n_problems,
     MK(cudaMemcpyAsync(S->vstage.p, vals, n * n_problems * 8, cudaMemcpyDefault, S->s));
     MK(cudaMemsetAsync(S->vmax.p, 0, 8 * (size_t)n_problems, S->s));
     k_absmax_vals<<<dim3(std::min(nblk((uint32_t)n), 1024u), n_problems), kT, 0, S->s>>>(
-        S->vstage.p, S->fixed.p, (uint32_t)n, n, S->vmax.p);
+        S->vstage.p, S->fixed.p, (uint32_t)n, n, S->vmax.p, S->lv[0].G.mnat);
     MK(cudaGetLastError());
     std::vector<unsigned long long> mb(n_problems);
     MK(cudaMemcpyAsync(mb.data(), S->vmax.p, 8 * (size_t)n_problems, cudaMemcpyDeviceToHost,
@@ -2621,7 +2705,7 @@ int ig_mixed_solve_values(void* handle, const double* vals, int n_problems,
     for (int b = 0; b < n_problems; b++) vm[b] = bits_to_double(mb[b]);
     set_units(*S, vm);
     k_init_vals<<<dim3(nblk((uint32_t)n), n_problems), kT, 0, S->s>>>(
-        S->phi.p, S->fixed.p, S->vstage.p, (uint32_t)n, n, S->fexp.p);
+        S->phi.p, S->fixed.p, S->vstage.p, (uint32_t)n, n, S->fexp.p, S->lv[0].G.mnat);
     MK(cudaGetLastError());
     g_mixed_launches.fetch_add(2);
     const MixedResult r = run_mixed(*S, acc, max_steps);

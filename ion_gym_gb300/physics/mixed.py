@@ -51,10 +51,11 @@ def cycle_for(max_problems):
     return dict(CYCLE_BATCH if int(max_problems) >= BATCH_MIN else CYCLE_SINGLE)
 
 
-def session_bytes(shape, max_problems):
-    """Device bytes a MixedSession of this grid and batch holds."""
-    return int(_lib.lib().ig_mixed_bytes(*[int(s) for s in shape],
-                                         int(max_problems)))
+def session_bytes(shape, max_problems, per_problem=False):
+    """Device bytes a MixedSession of this grid and batch holds
+    (per_problem: one metal per problem)."""
+    fn = _lib.lib().ig_mixed_bytes_multi if per_problem else _lib.lib().ig_mixed_bytes
+    return int(fn(*[int(s) for s in shape], int(max_problems)))
 
 
 class MixedSession:
@@ -64,26 +65,42 @@ class MixedSession:
     sessions of different geometries, driven from different host threads,
     run concurrently on the device."""
 
-    def __init__(self, metal, max_problems, stencil="ghost_linear", **cycle):
-        """cycle: overrides of the batch-size default (`cycle_for`): nu1,
+    def __init__(self, metal, max_problems=None, stencil="ghost_linear", **cycle):
+        """metal: the (nx, ny, nz) metal union every problem shares, or a
+        (P, nx, ny, nz) stack of one metal per problem (decks of one grid
+        shape solved as one batch with solve_values; max_problems is then
+        P).  cycle: overrides of the batch-size default (`cycle_for`): nu1,
         nu2, vcycles, gamma, gamma_levels, smooth_omega, method,
         cg_iters."""
-        metal = np.asarray(metal, bool)
-        self.shape = metal.shape
-        self.max_problems = int(max_problems)
+        metal = np.ascontiguousarray(np.asarray(metal, bool))
+        self.per_problem = metal.ndim == 4
+        if self.per_problem:
+            self.shape = metal.shape[1:]
+            self.max_problems = int(metal.shape[0])
+            if max_problems not in (None, self.max_problems):
+                raise ValueError("MixedSession: a stack of metals sets max_problems")
+        else:
+            if max_problems is None:
+                raise TypeError("MixedSession: max_problems is required with one metal")
+            self.shape = metal.shape
+            self.max_problems = int(max_problems)
         unknown = set(cycle) - set(CYCLE_SINGLE)
         if unknown:
             raise TypeError(f"MixedSession: unknown cycle settings {sorted(unknown)}")
         self.cycle = {**cycle_for(self.max_problems), **cycle}
         c = self.cycle
-        self.nbytes = session_bytes(self.shape, self.max_problems)
+        self.nbytes = session_bytes(self.shape, self.max_problems, self.per_problem)
         self._h = ctypes.c_void_p(None)
-        st = _lib.lib().ig_mixed_open_ex(
-            ptr(as_mask(metal)), *self.shape, self.max_problems,
-            stencil_code(stencil), int(c["nu1"]), int(c["nu2"]),
-            int(c["vcycles"]), int(c["gamma"]), int(c["gamma_levels"]),
-            float(c["smooth_omega"]), int(c["method"]), int(c["cg_iters"]),
-            ctypes.byref(self._h))
+        args = (stencil_code(stencil), int(c["nu1"]), int(c["nu2"]),
+                int(c["vcycles"]), int(c["gamma"]), int(c["gamma_levels"]),
+                float(c["smooth_omega"]), int(c["method"]), int(c["cg_iters"]),
+                ctypes.byref(self._h))
+        if self.per_problem:
+            st = _lib.lib().ig_mixed_open_multi(ptr(as_mask(metal)), self.max_problems,
+                                                *self.shape, *args)
+        else:
+            st = _lib.lib().ig_mixed_open_ex(ptr(as_mask(metal)), *self.shape,
+                                             self.max_problems, *args)
         _lib.check(st, "MixedSession")
 
     def _outcome(self, st, steps, dmax, accuracy, span):
@@ -143,12 +160,14 @@ class MixedSession:
 
     def solve_values(self, vals, accuracy=1e-9, max_steps=40, out=None,
                      span=None):
-        """vals: (P, nx, ny, nz) Dirichlet values (read at the metal nodes)
+        """vals: (P, nx, ny, nz) Dirichlet values (read at the metal nodes;
+        on a session with one metal per problem, problem p's on metal p)
         -> array (P, nx, ny, nz); accuracy is relative to the span of the
         Dirichlet values (max - min of vals, at least 1 V; pass `span` when
-        it is known, to skip the host pass over vals).  `out`: a
-        C-contiguous float64 array of that shape to fill (pinned host memory
-        makes the download fast)."""
+        it is known, to skip the host pass over vals; a sequence of P spans
+        gives each problem its own accuracy).  `out`: a C-contiguous
+        float64 array of that shape to fill (pinned host memory makes the
+        download fast)."""
         vals = np.ascontiguousarray(vals, np.float64)
         if vals.ndim == 3:
             vals = vals[None]
@@ -163,10 +182,20 @@ class MixedSession:
             phi = out.reshape(vals.shape)
         steps = ctypes.c_int(0)
         dmax = np.zeros(P)
-        span = max(float(np.ptp(vals)) if span is None else float(span), 1.0)
-        st = _lib.lib().ig_mixed_solve_values(
-            self._h, ptr(vals), P, float(accuracy) * span, int(max_steps),
-            ptr(phi), ctypes.byref(steps), ptr(dmax))
+        if span is not None and np.ndim(span) == 1:
+            spans = np.maximum(np.asarray(span, np.float64), 1.0)
+            if spans.shape != (P,):
+                raise ValueError(f"solve_values: {spans.shape[0]} spans for {P} problems")
+            accs = np.ascontiguousarray(float(accuracy) * spans)
+            st = _lib.lib().ig_mixed_solve_values_acc(
+                self._h, ptr(vals), P, ptr(accs), int(max_steps), ptr(phi),
+                ctypes.byref(steps), ptr(dmax))
+            span = float(spans.min())
+        else:
+            span = max(float(np.ptp(vals)) if span is None else float(span), 1.0)
+            st = _lib.lib().ig_mixed_solve_values(
+                self._h, ptr(vals), P, float(accuracy) * span, int(max_steps),
+                ptr(phi), ctypes.byref(steps), ptr(dmax))
         self._outcome(st, steps.value, dmax, accuracy, span)
         self.last_steps = int(steps.value)
         return phi
@@ -177,10 +206,12 @@ class MixedSession:
         device buffers, the tuned smoother and the captured CUDA graphs are
         kept -- a solve after rebind costs no session build.  Results equal
         those of a session opened on the new metal."""
-        metal = np.asarray(metal, bool)
-        if metal.shape != self.shape:
+        metal = np.ascontiguousarray(np.asarray(metal, bool))
+        want = ((self.max_problems,) + tuple(self.shape) if self.per_problem
+                else tuple(self.shape))
+        if metal.shape != want:
             raise ValueError(f"rebind: metal of shape {metal.shape}, session "
-                             f"shape {self.shape}")
+                             f"shape {want}")
         st = _lib.lib().ig_mixed_rebind(self._h, ptr(as_mask(metal)), *self.shape)
         _lib.check(st, "MixedSession.rebind")
         return self
