@@ -231,6 +231,13 @@ int ig_mixed_time_gs(void *handle, int n_problems, int pairs,
  * this gives the whole step's achieved bandwidth.  No reference
  * counterpart (a measurement aid). */
 int ig_mixed_step_bytes(void *handle, int n_problems, double *bytes_out);
+/* Checks the integer-pipe float -> int64 conversion (round to nearest
+ * even) that the mixed path's update uses to add a correction to the
+ * fixed-point potential against the GPU's own conversion instruction, bit
+ * for bit, on n host values (copied to the device): *mismatches = the
+ * number of values whose results differ, 0 when all agree.  No reference
+ * counterpart (a self-check of this library). */
+int ig_mixed_check_convert(const float *floats, long n, long long *mismatches);
 /* Checks the fused kernels of the mixed path against the separate launches
  * they replace, on the state the session's last solve left (right-hand
  * sides, corrections, direction): mismatches[0] = the first Gauss-Seidel

@@ -182,15 +182,16 @@ __device__ __forceinline__ void gs4_at(float* __restrict__ own, const float* __r
   const int p = (i + j + c) & 1;
   const uint32_t base = ij * (uint32_t)G.H + m0;
   const uchar4 mk = *reinterpret_cast<const uchar4*>(mp + base);
-  if (mk.x & mk.y & mk.z & mk.w) return;  // all metal or unused slots
-  const float4 gg = ld4(gp + base);
   float q[4];
   // Grids with no size-1 axis take the float4 path for every group, the z
   // faces included, so no warp diverges into a per-slot path at the ends of
-  // its rows.
-  if (!FLAT) {
-    nbr4(PlainLd{oth}, G, i, j, m0, p, base, q);
-  } else {
+  // its rows.  There the loads (in bounds in every group) are issued with
+  // the mask's rather than after it, so a group waits for one memory round
+  // trip, not two.
+  const float4 gg = ld4(gp + base);
+  if (!FLAT) nbr4(PlainLd{oth}, G, i, j, m0, p, base, q);
+  if (mk.x & mk.y & mk.z & mk.w) return;  // all metal or unused slots
+  if (FLAT) {
 #pragma unroll
     for (int u = 0; u < 4; u++) {
       const int k = 2 * (m0 + u) + p;
@@ -634,11 +635,9 @@ k_resid0_4(const float* __restrict__ e, const float* __restrict__ g,
   const int j = (int)(ij - (uint32_t)i * G.dny.d);
   const uint32_t base = ij * (uint32_t)G.H + m0;
   float4* out = reinterpret_cast<float4*>(r + blockIdx.y * (size_t)G.csz + base);
+  // no early exit on an all-metal group: the loads are in bounds in every
+  // group and go out with the mask's; metal slots select 0 below
   const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + base);
-  if (mk.x & mk.y & mk.z & mk.w) {
-    *out = make_float4(0.f, 0.f, 0.f, 0.f);
-    return;
-  }
   const float* eb = e + blockIdx.y * pstride;
   float q[4];
   nbr4(PlainLd{eb + G.csz}, G, i, j, m0, (i + j) & 1, base, q);
@@ -923,6 +922,7 @@ k_prolong_add4_gather(const float* __restrict__ ec, SGeo C, float* __restrict__ 
       }
     add[u] = acc;
   }
+  if (mk.x & mk.y & mk.z & mk.w) return;  // metal or unused: nothing to add
   float4* out = reinterpret_cast<float4*>(ef + fstride * blockIdx.y + (size_t)c * F.csz + base);
   float4 v = *out;
   v.x += add[0];
@@ -955,8 +955,9 @@ k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
   const int j = (int)(ij - (uint32_t)i * F.dny.d);
   const int pc = (i + j + c) & 1;
   const uint32_t base = ij * (uint32_t)F.H + m0;
+  // the coarse values are fetched whatever the mask says (in bounds); an
+  // all-metal (or unused) group skips only the read-modify-write below
   const uchar4 mk = *reinterpret_cast<const uchar4*>(maskf + (size_t)c * F.csz + base);
-  if (mk.x & mk.y & mk.z & mk.w) return;  // metal or unused: nothing to add
   const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
   const float* eb = ec + blockIdx.y * cstride;
   const LerpF x = pa(i, C.nx), y = pa(j, C.ny);
@@ -1005,6 +1006,7 @@ k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
         acc[u] += w * zs;
       }
     }
+  if (mk.x & mk.y & mk.z & mk.w) return;  // metal or unused: nothing to add
   float4* out = reinterpret_cast<float4*>(ef + fstride * blockIdx.y + (size_t)c * F.csz + base);
   float4 v = *out;
   v.x += mv[0] ? 0.f : acc[0];
@@ -1155,40 +1157,79 @@ __device__ __forceinline__ double pow2d(int k) {
   return __longlong_as_double(static_cast<long long>(1023 + k) << 52);
 }
 
+// RN(x) as an int64 on the integer pipe (the hardware conversion runs on
+// the FP64 pipe, which this GPU has little of): the IEEE conversion itself,
+// rounded once to nearest, ties to even, from the discarded bits and the
+// kept integer's last bit.  |x| >= 2^63, infinities and NaN take the
+// hardware conversion.  Checked against it bit for bit by
+// ig_mixed_check_convert.
+__device__ __forceinline__ long long f2ll_rn(float x) {
+  const unsigned b = __float_as_uint(x);
+  const int ef = static_cast<int>((b >> 23) & 0xffu);
+  if (ef < 126) return 0LL;  // |x| < 1/2 (zeros and subnormals included)
+  if (ef >= 190) return __float2ll_rn(x);
+  const unsigned long long m = (b & 0x7fffffu) | 0x800000u;  // |x| = m * 2^(ef - 150)
+  unsigned long long r;
+  if (ef >= 150) {
+    r = m << (ef - 150);
+  } else {
+    const int sh = 150 - ef;  // 1..24
+    r = m >> sh;
+    const unsigned long long rem = m & ((1ULL << sh) - 1ULL), half = 1ULL << (sh - 1);
+    r += (rem > half || (rem == half && (r & 1ULL))) ? 1ULL : 0ULL;
+  }
+  return (b >> 31) ? -static_cast<long long>(r) : static_cast<long long>(r);
+}
+
 // g32 = -(float) (scale * r(phi)) at free nodes, 0 at metal; r is the
 // reference's fine residual with theta None (kind kPlain: sum - 6 phi; the
 // Shortley-Weller form is half of it and is scaled by 2 through nscale =
 // -(float) scale, a power of two).  The residual is an exact int64 sum of
 // the fixed-point potentials, rounded once to float and scaled by u_b.
+// One warp per natural row (i, j): the row's coordinates, its four x/y
+// neighbour rows and its two split output rows are worked out once, and
+// the lanes walk the row 32 nodes at a time (two steps in flight), so every
+// load of the row and of its neighbour rows is 256 contiguous bytes.
+constexpr int kRowWarps = kT / 32;
+inline unsigned rows_blocks(const SGeo& g) {
+  return (unsigned)(((size_t)g.nx * g.ny + kRowWarps - 1) / kRowWarps);
+}
 __global__ void __launch_bounds__(kT)
 k_resid64(const long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
           SGeo G, float* __restrict__ g, const int* __restrict__ fexp, float nscale,
           size_t nstride, size_t pstride) {
-  fixed += (size_t)blockIdx.y * G.mnat;
-  const uint32_t t = blockIdx.x * kT + threadIdx.x;
-  if (t >= G.n) return;
-  const uint32_t ij = fdivu(t, G.dnz);
-  const int k = (int)(t - ij * G.dnz.d);
-  const int i = (int)fdivu(ij, G.dny);
-  const int j = (int)(ij - (uint32_t)i * G.dny.d);
-  float out = 0.f;
-  if (!fixed[t]) {
-    const long long* p = phi + blockIdx.y * nstride;
-    const uint32_t sx = (uint32_t)G.ny * G.nz, sy = G.nz;
-    const uint32_t row = (uint32_t)i * sx + (uint32_t)j * sy;
-    const long long s =
-        ((p[(uint32_t)lo_i(i, G.nx) * sx + (uint32_t)j * sy + k] +
-          p[(uint32_t)hi_i(i, G.nx) * sx + (uint32_t)j * sy + k]) +
-         (p[(uint32_t)i * sx + (uint32_t)lo_i(j, G.ny) * sy + k] +
-          p[(uint32_t)i * sx + (uint32_t)hi_i(j, G.ny) * sy + k])) +
-        (p[row + lo_i(k, G.nz)] + p[row + hi_i(k, G.nz)]);
-    const long long c = p[t];
-    const long long r = s - ((c << 2) + (c << 1));
-    out = __ll2float_rn(r) * pow2f(fexp[blockIdx.y] - 56) * nscale;
+  const uint32_t r = blockIdx.x * kRowWarps + (threadIdx.x >> 5);
+  if (r >= (uint32_t)G.nx * (uint32_t)G.ny) return;  // whole warps
+  const int lane = threadIdx.x & 31;
+  const int i = (int)fdivu(r, G.dny);
+  const int j = (int)(r - (uint32_t)i * G.dny.d);
+  const int nz = G.nz;
+  const long long* p = phi + blockIdx.y * nstride;
+  const long long* pr = p + (size_t)r * nz;
+  const long long* pxm = p + ((size_t)lo_i(i, G.nx) * G.ny + j) * nz;
+  const long long* pxp = p + ((size_t)hi_i(i, G.nx) * G.ny + j) * nz;
+  const long long* pym = p + ((size_t)i * G.ny + lo_i(j, G.ny)) * nz;
+  const long long* pyp = p + ((size_t)i * G.ny + hi_i(j, G.ny)) * nz;
+  const uint8_t* fr = fixed + (size_t)blockIdx.y * G.mnat + (size_t)r * nz;
+  // the colour of the row's even k, then the split rows of both colours
+  const int ce = (i + j) & 1;
+  float* gb = g + blockIdx.y * pstride + (size_t)r * G.H;
+  float* ge = gb + (size_t)ce * G.csz;
+  float* go = gb + (size_t)(1 - ce) * G.csz;
+  const float u = pow2f(fexp[blockIdx.y] - 56);
+  // every load is in bounds whatever the mask says, so the mask and the
+  // seven potentials are fetched together and the mask only selects
+#pragma unroll 2
+  for (int k = lane; k < nz; k += 32) {
+    const int km = k > 0 ? k - 1 : (nz > 1 ? 1 : k);
+    const int kp = k + 1 < nz ? k + 1 : (nz > 1 ? nz - 2 : k);
+    const uint8_t metal = fr[k];
+    const long long s = ((pxm[k] + pxp[k]) + (pym[k] + pyp[k])) + (pr[km] + pr[kp]);
+    const long long c = pr[k];
+    const long long rr = s - ((c << 2) + (c << 1));
+    ((k & 1) ? go : ge)[k >> 1] = metal ? 0.f : __ll2float_rn(rr) * u * nscale;
   }
-  g[blockIdx.y * pstride + (size_t)scol(i, j, k) * G.csz + sidx(G, i, j, k)] = out;
 }
-
 
 // float -> double by its bits for zeros and normal floats (exponent rebias,
 // significand moved up 29 bits); subnormals, infinities and NaN convert on
@@ -1209,82 +1250,52 @@ __device__ __forceinline__ double widen(float d) {
 // Phi += e32 / u_b (rounded to the nearest unit) at free nodes; the
 // per-problem maximum of |e32| (the applied change, to within half a unit)
 // goes to dmax[b] as float64 bits (the refinement's convergence norm, the
-// analogue of the V-cycle's full-cycle change, multigrid3d.py:702).  Eight
-// consecutive natural nodes
-// k0 = 8g .. 8g+7 of one row per thread: their corrections are float4 group
-// g of each colour's split row (k0 is even, so colour (i + j) & 1 holds k0,
-// k0+2, .. and the other colour k0+1, k0+3, ..), the potentials and masks
-// 64 and 8 contiguous bytes.  One block maximum per 2048 nodes.
+// analogue of the V-cycle's full-cycle change, multigrid3d.py:702).  With
+// p given, e32 is e + alpha p: the flexible CG's last step x += alpha p
+// folded in (k_cg_update's expression; its g half is dead, the residual is
+// recomputed next).  One warp per natural row, as k_resid64: lane k's
+// potential and mask are 8 and 1 contiguous bytes of the row, its
+// correction slot k >> 1 of the colour (i + j + k) & 1, so a warp's loads
+// of the corrections are two runs of 16 consecutive floats.
 __global__ void __launch_bounds__(kT)
-k_update64_8(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
-             const float* __restrict__ e, SGeo G, unsigned long long* dmax,
-             const int* __restrict__ fexp, size_t nstride, size_t pstride,
-             const float* __restrict__ p = nullptr, const double* __restrict__ scal = nullptr) {
-  fixed += (size_t)blockIdx.y * G.mnat;
-  // The block's groups cover one contiguous natural range [n_lo, n_hi) (a
-  // row's valid groups are consecutive and the next row starts where it
-  // ends; groups past a row's end cover nothing), at most 8 kT nodes: the
-  // potentials and masks of that range go through shared memory, so global
-  // loads and stores are coalesced whole rows instead of 64-byte pieces per
-  // thread.
-  __shared__ long long sphi[kT * 8];
-  __shared__ uint8_t sfix[kT * 8];
-  const uint32_t ngroups = G.csz >> 2;
-  const uint32_t H4 = G.dH4.d;
-  const uint32_t t0 = blockIdx.x * kT;
-  const uint32_t t1 = min(t0 + kT, ngroups) - 1;
-  const uint32_t ij0 = fdivu(t0, G.dH4), ij1 = fdivu(t1, G.dH4);
-  const uint32_t k00 = 8 * (t0 - ij0 * H4), k01 = 8 * (t1 - ij1 * H4);
-  const uint32_t nz = (uint32_t)G.nz;
-  const uint32_t n_lo = k00 < nz ? ij0 * nz + k00 : (ij0 + 1) * nz;
-  const uint32_t n_hi = k01 < nz ? min(ij1 * nz + k01 + 8, (ij1 + 1) * nz) : (ij1 + 1) * nz;
-  const uint32_t span = n_hi > n_lo ? n_hi - n_lo : 0;
-  long long* P = phi + blockIdx.y * nstride;
-  const float to_units = pow2f(56 - fexp[blockIdx.y]);
-  for (uint32_t q = threadIdx.x; q < span; q += kT) {
-    sphi[q] = P[n_lo + q];
-    sfix[q] = fixed[n_lo + q];
-  }
-  __syncthreads();
-  const uint32_t t = t0 + threadIdx.x;
+k_update64(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
+           const float* __restrict__ e, SGeo G, unsigned long long* dmax,
+           const int* __restrict__ fexp, size_t nstride, size_t pstride,
+           const float* __restrict__ p = nullptr, const double* __restrict__ scal = nullptr) {
+  const uint32_t r = blockIdx.x * kRowWarps + (threadIdx.x >> 5);
   unsigned long long key = 0;
-  if (t < ngroups) {
-    const uint32_t ij = fdivu(t, G.dH4);
-    const int k0 = 8 * (int)(t - ij * H4);
-    if (k0 < G.nz) {
-      const int i = (int)fdivu(ij, G.dny);
-      const int j = (int)(ij - (uint32_t)i * G.dny.d);
-      const int p0 = (i + j) & 1;
-      const float* eb = e ? e + blockIdx.y * pstride + ij * (uint32_t)G.H + (k0 >> 1) : nullptr;
-      float4 ea = e ? ld4(eb + (size_t)p0 * G.csz) : make_float4(0.f, 0.f, 0.f, 0.f);
-      float4 eo = e ? ld4(eb + (size_t)(1 - p0) * G.csz) : make_float4(0.f, 0.f, 0.f, 0.f);
-      if (p) {
-        // the flexible CG's last step x += alpha p, folded in (k_cg_update's
-        // expression; its g half is dead: the residual is recomputed next)
-        const float al = (float)scal[4 * blockIdx.y + 1];
-        const float* pb = p + blockIdx.y * pstride + ij * (uint32_t)G.H + (k0 >> 1);
-        const float4 pa = ld4(pb + (size_t)p0 * G.csz), po = ld4(pb + (size_t)(1 - p0) * G.csz);
-        ea.x = __fmaf_rn(al, pa.x, ea.x); ea.y = __fmaf_rn(al, pa.y, ea.y);
-        ea.z = __fmaf_rn(al, pa.z, ea.z); ea.w = __fmaf_rn(al, pa.w, ea.w);
-        eo.x = __fmaf_rn(al, po.x, eo.x); eo.y = __fmaf_rn(al, po.y, eo.y);
-        eo.z = __fmaf_rn(al, po.z, eo.z); eo.w = __fmaf_rn(al, po.w, eo.w);
-      }
-      const float ev[8] = {ea.x, eo.x, ea.y, eo.y, ea.z, eo.z, ea.w, eo.w};
-      const uint32_t off = ij * nz + (uint32_t)k0 - n_lo;
-#pragma unroll
-      for (int u = 0; u < 8; u++) {
-        if (k0 + u >= G.nz || sfix[off + u]) continue;
-        const double dd = widen(ev[u]);
-        sphi[off + u] = sphi[off + u] + __float2ll_rn(ev[u] * to_units);
-        unsigned long long kk =
-            static_cast<unsigned long long>(__double_as_longlong(dd)) & 0x7fffffffffffffffULL;
-        if (kk > 0x7ff0000000000000ULL) kk = 0x7ff0000000000000ULL;  // NaN: never converged
-        key = max(key, kk);
-      }
+  if (r < (uint32_t)G.nx * (uint32_t)G.ny) {
+    const int lane = threadIdx.x & 31;
+    const int i = (int)fdivu(r, G.dny);
+    const int j = (int)(r - (uint32_t)i * G.dny.d);
+    const int nz = G.nz;
+    long long* pr = phi + blockIdx.y * nstride + (size_t)r * nz;
+    const uint8_t* fr = fixed + (size_t)blockIdx.y * G.mnat + (size_t)r * nz;
+    const size_t ro = blockIdx.y * pstride + (size_t)r * G.H;
+    const float* ee = e ? e + ro + (size_t)((i + j) & 1) * G.csz : nullptr;
+    const float* eo = e ? e + ro + (size_t)(1 - ((i + j) & 1)) * G.csz : nullptr;
+    const float* pe = p ? p + ro + (size_t)((i + j) & 1) * G.csz : nullptr;
+    const float* po = p ? p + ro + (size_t)(1 - ((i + j) & 1)) * G.csz : nullptr;
+    const float al = p ? (float)scal[4 * blockIdx.y + 1] : 0.f;
+    const float to_units = pow2f(56 - fexp[blockIdx.y]);
+    // the loads do not wait for the mask (all in bounds), and every node
+    // is written back (metal nodes unchanged), so no lane branches
+#pragma unroll 2
+    for (int k = lane; k < nz; k += 32) {
+      const int m = k >> 1;
+      const uint8_t metal = fr[k];
+      const long long old = pr[k];
+      float ev = e ? ((k & 1) ? eo : ee)[m] : 0.f;
+      if (p) ev = __fmaf_rn(al, ((k & 1) ? po : pe)[m], ev);
+      ev = metal ? 0.f : ev;
+      pr[k] = old + f2ll_rn(ev * to_units);
+      unsigned long long kk =
+          static_cast<unsigned long long>(__double_as_longlong(widen(ev))) &
+          0x7fffffffffffffffULL;
+      if (kk > 0x7ff0000000000000ULL) kk = 0x7ff0000000000000ULL;  // NaN: never converged
+      key = max(key, kk);
     }
   }
-  __syncthreads();
-  for (uint32_t q = threadIdx.x; q < span; q += kT) P[n_lo + q] = sphi[q];
   block_max_to(key, dmax + blockIdx.y);
 }
 
@@ -1339,12 +1350,22 @@ __global__ void k_fixed_out(long long* __restrict__ phi, const uint8_t* __restri
   if (t >= n) return;
   fixed += blockIdx.y * fstride;
   const size_t o = blockIdx.y * nstride + t;
-  double r;
-  if (fixed[t])
-    r = vals ? vals[o] : (masks[(size_t)blockIdx.y * n + t] ? v : 0.0);
-  else
-    r = __ll2double_rn(phi[o]) * pow2d(fexp[blockIdx.y] - 56);
+  // the potential is fetched with the mask, not after it; only metal nodes
+  // (few) wait for their Dirichlet value
+  const long long q = phi[o];
+  const uint8_t metal = fixed[t];
+  double r = __ll2double_rn(q) * pow2d(fexp[blockIdx.y] - 56);
+  if (metal) r = vals ? vals[o] : (masks[(size_t)blockIdx.y * n + t] ? v : 0.0);
   reinterpret_cast<double*>(phi)[o] = r;
+}
+
+// f2ll_rn against the hardware conversion: mism counts the inputs whose
+// results differ.
+__global__ void k_check_convert(const float* __restrict__ fv, uint32_t n,
+                                unsigned long long* mism) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= n) return;
+  if (f2ll_rn(fv[t]) != __float2ll_rn(fv[t])) atomicAdd(mism, 1ULL);
 }
 
 // ---- flexible CG on the FP32 correction (level 0, split layout) --------
@@ -1397,19 +1418,23 @@ struct KSum {
 };
 
 // q = L p (both colours; q = 0 on metal) and block partials of <p, q> and
-// <p, g>; blockIdx.z = colour.  Grid-stride over float4 groups (kCgBlocks
-// blocks per colour and problem), so each block reduces once.
+// <p, g>; blockIdx.y = colour, blockIdx.z = problem.  Grid-stride over
+// float4 groups (kCgBlocks blocks per colour and problem), so each block
+// reduces once.  Blocks start in (x, y, z) order, so the two colours of a
+// problem run side by side over the same rows: the other colour's values
+// one colour reads as neighbours are the ones the other is reading as its
+// own, and come from L2 rather than from a second pass over DRAM.
 constexpr unsigned kCgBlocks = 152 * 2;
 __global__ void __launch_bounds__(kT)
 k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
             const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ q,
             double* __restrict__ part, size_t pstride) {
-  mask += (size_t)blockIdx.y * G.msplit;
+  mask += (size_t)blockIdx.z * G.msplit;
   __shared__ double sh[kT / 32];
-  const int c = blockIdx.z;
+  const int c = blockIdx.y;
   const uint32_t nq = G.csz >> 2;
   KSum spq, spg;
-  const float* pb = p + blockIdx.y * pstride;
+  const float* pb = p + blockIdx.z * pstride;
   const float* own = pb + (size_t)c * G.csz;
   const float* oth = pb + (size_t)(1 - c) * G.csz;
   for (uint32_t t = blockIdx.x * kT + threadIdx.x; t < nq; t += gridDim.x * kT) {
@@ -1422,7 +1447,7 @@ k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
     const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + (size_t)c * G.csz + base);
     const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
     const float4 pv = ld4(own + base);
-    const float4 gv = ld4(g + blockIdx.y * pstride + (size_t)c * G.csz + base);
+    const float4 gv = ld4(g + blockIdx.z * pstride + (size_t)c * G.csz + base);
     const float pp[4] = {pv.x, pv.y, pv.z, pv.w};
     const float gg[4] = {gv.x, gv.y, gv.z, gv.w};
     float out[4];
@@ -1435,14 +1460,14 @@ k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
       spq.add(pp[u] * out[u]);
       spg.add(pp[u] * gg[u]);
     }
-    *reinterpret_cast<float4*>(q + blockIdx.y * pstride + (size_t)c * G.csz + base) =
+    *reinterpret_cast<float4*>(q + blockIdx.z * pstride + (size_t)c * G.csz + base) =
         make_float4(out[0], out[1], out[2], out[3]);
   }
   const double a = block_sum_d(spq.value(), sh);
   __syncthreads();
   const double b = block_sum_d(spg.value(), sh);
   if (threadIdx.x == 0) {
-    const size_t slot = ((size_t)blockIdx.y * 2 + c) * gridDim.x + blockIdx.x;
+    const size_t slot = ((size_t)blockIdx.z * 2 + c) * gridDim.x + blockIdx.x;
     part[2 * slot] = a;
     part[2 * slot + 1] = b;
   }
@@ -1453,20 +1478,21 @@ k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
 // own slots (stored to pn) and at their six neighbours -- so z and p_old are
 // read once and p is written once.  p_old and pn are different arrays (a
 // thread of one colour reads the other colour's p_old while that colour's
-// threads store theirs).  Same expressions as the two kernels, same bits.
+// threads store theirs).  Same expressions as the two kernels, same bits;
+// the same grid (colour in y, problem in z).
 __global__ void __launch_bounds__(kT, 4)
 k_cg_matvec_dir(const float* __restrict__ z, const float* __restrict__ po,
                 float* __restrict__ pn, const double* __restrict__ scal,
                 const float* __restrict__ g, const uint8_t* __restrict__ mask, SGeo G,
                 float* __restrict__ q, double* __restrict__ part, size_t pstride) {
-  mask += (size_t)blockIdx.y * G.msplit;
+  mask += (size_t)blockIdx.z * G.msplit;
   __shared__ double sh[kT / 32];
-  const int c = blockIdx.z;
+  const int c = blockIdx.y;
   const uint32_t nq = G.csz >> 2;
-  const float b = (float)scal[4 * blockIdx.y + 2];
+  const float b = (float)scal[4 * blockIdx.z + 2];
   KSum spq, spg;
-  const size_t own = blockIdx.y * pstride + (size_t)c * G.csz;
-  const size_t oth = blockIdx.y * pstride + (size_t)(1 - c) * G.csz;
+  const size_t own = blockIdx.z * pstride + (size_t)c * G.csz;
+  const size_t oth = blockIdx.z * pstride + (size_t)(1 - c) * G.csz;
   const DirLd on{z + oth, po + oth, b};
   for (uint32_t t = blockIdx.x * kT + threadIdx.x; t < nq; t += gridDim.x * kT) {
     const uint32_t ij = fdivu(t, G.dH4);
@@ -1482,14 +1508,12 @@ k_cg_matvec_dir(const float* __restrict__ z, const float* __restrict__ po,
     const float4 gv = ld4(g + own + base);
     const float pp[4] = {pv.x, pv.y, pv.z, pv.w};
     const float gg[4] = {gv.x, gv.y, gv.z, gv.w};
-    float out[4] = {0.f, 0.f, 0.f, 0.f};
-    if (!(mk.x & mk.y & mk.z & mk.w)) {
-      float nb[4];
-      nbr4(on, G, i, j, m0, pc, base, nb);
+    // the neighbour loads (in bounds in every group, padding included) do
+    // not wait for the mask; it only selects
+    float nb[4], out[4];
+    nbr4(on, G, i, j, m0, pc, base, nb);
 #pragma unroll
-      for (int u = 0; u < 4; u++)
-        if (!mv[u]) out[u] = 6.0f * pp[u] - nb[u];
-    }
+    for (int u = 0; u < 4; u++) out[u] = mv[u] ? 0.f : 6.0f * pp[u] - nb[u];
 #pragma unroll
     for (int u = 0; u < 4; u++) {
       spq.add(pp[u] * out[u]);
@@ -1501,7 +1525,7 @@ k_cg_matvec_dir(const float* __restrict__ z, const float* __restrict__ po,
   __syncthreads();
   const double bb = block_sum_d(spg.value(), sh);
   if (threadIdx.x == 0) {
-    const size_t slot = ((size_t)blockIdx.y * 2 + c) * gridDim.x + blockIdx.x;
+    const size_t slot = ((size_t)blockIdx.z * 2 + c) * gridDim.x + blockIdx.x;
     part[2 * slot] = a;
     part[2 * slot + 1] = bb;
   }
@@ -2021,19 +2045,19 @@ struct Session {
   void step_enqueue() {
     MLevel& f = lv[0];
     const size_t nstride = f.G.n;
-    const dim3 gn(nblk(f.G.n), B);
+    const dim3 gn(rows_blocks(f.G), B);
     k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, fexp.p, (float)-resid_scale, nstride,
                                 f.pstride);
     for (int v = 0; v < vcycles; v++) vcycle(0, v == 0);
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
-    k_update64_8<<<dim3(nblk(f.G.csz / 4), B), kT, 0, s>>>(phi.p, fixed.p, f.e.p, f.G, dmax.p,
+    k_update64<<<dim3(rows_blocks(f.G), B), kT, 0, s>>>(phi.p, fixed.p, f.e.p, f.G, dmax.p,
                                                          fexp.p, nstride, f.pstride);
   }
 
   // the flexible CG: once per solve, the FP64 residual and zero state
   void cg_init() {
     MLevel& f = lv[0];
-    const dim3 gn(nblk(f.G.n), B);
+    const dim3 gn(rows_blocks(f.G), B);
     k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, fexp.p, (float)-resid_scale, f.G.n,
                                 f.pstride);
     MK(cudaMemsetAsync(xb.p, 0, f.pstride * B * 4, s));
@@ -2059,12 +2083,12 @@ struct Session {
       k_cg_dot<<<dim3(nbd, B), kT, 0, s>>>(f.e.p, qb.p, part.p, f.pstride, n);
       k_cg_reduce<<<B, kT, 0, s>>>(part.p, (int)nbd, 1, scal.p, 1);
       if (fuse_dir()) {
-        k_cg_matvec_dir<<<dim3(nb4, B, 2), kT, 0, s>>>(f.e.p, pcur, pnext, scal.p, f.g.p,
+        k_cg_matvec_dir<<<dim3(nb4, 2, B), kT, 0, s>>>(f.e.p, pcur, pnext, scal.p, f.g.p,
                                                       f.mask.p, f.G, qb.p, part.p, f.pstride);
         std::swap(pcur, pnext);
       } else {
         k_cg_dir<<<gv, kT, 0, s>>>(pcur, f.e.p, scal.p, f.pstride, n);
-        k_cg_matvec<<<dim3(nb4, B, 2), kT, 0, s>>>(pcur, f.g.p, f.mask.p, f.G, qb.p, part.p,
+        k_cg_matvec<<<dim3(nb4, 2, B), kT, 0, s>>>(pcur, f.g.p, f.mask.p, f.G, qb.p, part.p,
                                                   f.pstride);
       }
       k_cg_reduce<<<B, kT, 0, s>>>(part.p, 2 * (int)nb4, 2, scal.p, 0);
@@ -2077,10 +2101,10 @@ struct Session {
         k_cg_update<false><<<dim3(nblk(n / 4), B), kT, 0, s>>>(xb.p, f.g.p, pcur, qb.p, scal.p,
                                                               f.pstride, n);
     }
-    const dim3 gn(nblk(f.G.n), B);
+    const dim3 gn(rows_blocks(f.G), B);
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
     // phi += x + alpha p (x absent when the step has one iteration)
-    k_update64_8<<<dim3(nblk(f.G.csz / 4), B), kT, 0, s>>>(
+    k_update64<<<dim3(rows_blocks(f.G), B), kT, 0, s>>>(
         phi.p, fixed.p, cg_iters > 1 ? xb.p : nullptr, f.G, dmax.p, fexp.p, f.G.n, f.pstride,
         pcur, scal.p);
     k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, fexp.p, (float)-resid_scale, f.G.n,
@@ -2422,6 +2446,40 @@ int ig_mixed_rebind(void* handle, const uint8_t* metal, long nx, long ny, long n
   return IG_OK;
 }
 
+int ig_mixed_check_convert(const float* floats, long n, long long* mismatches) {
+  set_last_error("");
+  if (!floats || !mismatches || n < 1 || n > (1L << 30)) {
+    set_last_error("null argument or count outside 1..2^30");
+    return IG_BAD_ARG;
+  }
+  try {
+    cudaStream_t s = nullptr;
+    MK(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+    struct StreamGuard {
+      cudaStream_t s;
+      ~StreamGuard() {
+        cudaStreamSynchronize(s);
+        cudaStreamDestroy(s);
+      }
+    } guard{s};
+    Buf<float> fv;
+    Buf<unsigned long long> mm;
+    fv.alloc((size_t)n, s);
+    mm.alloc(1, s);
+    MK(cudaMemcpyAsync(fv.p, floats, 4 * (size_t)n, cudaMemcpyHostToDevice, s));
+    MK(cudaMemsetAsync(mm.p, 0, 8, s));
+    k_check_convert<<<nblk((uint32_t)n), kT, 0, s>>>(fv.p, (uint32_t)n, mm.p);
+    MK(cudaGetLastError());
+    unsigned long long h = 0;
+    MK(cudaMemcpyAsync(&h, mm.p, 8, cudaMemcpyDeviceToHost, s));
+    MK(cudaStreamSynchronize(s));
+    *mismatches = (long long)h;
+    return IG_OK;
+  } catch (int code) {
+    return code;
+  }
+}
+
 int ig_mixed_step_bytes(void* handle, int n_problems, double* bytes_out) {
   set_last_error("");
   Session* S = static_cast<Session*>(handle);
@@ -2573,12 +2631,12 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
       const size_t nparts = 2 * (size_t)B * 2 * nb4;
       Buf<double> part2;
       part2.alloc(nparts, s);
-      k_cg_matvec_dir<<<dim3(nb4, B, 2), kT, 0, s>>>(f.e.p, S->pb.p, S->pb2.p, S->scal.p,
+      k_cg_matvec_dir<<<dim3(nb4, 2, B), kT, 0, s>>>(f.e.p, S->pb.p, S->pb2.p, S->scal.p,
                                                     f.g.p, f.mask.p, f.G, scrB, part2.p,
                                                     f.pstride);
       k_cg_dir<<<dim3(nblk((uint32_t)f.pstride), B), kT, 0, s>>>(S->pb.p, f.e.p, S->scal.p,
                                                                  f.pstride, (uint32_t)f.pstride);
-      k_cg_matvec<<<dim3(nb4, B, 2), kT, 0, s>>>(S->pb.p, f.g.p, f.mask.p, f.G, scrA,
+      k_cg_matvec<<<dim3(nb4, 2, B), kT, 0, s>>>(S->pb.p, f.g.p, f.mask.p, f.G, scrA,
                                                 S->part.p, f.pstride);
       diff(S->pb.p, S->pb2.p, words, 3);
       diff(scrA, scrB, words, 3);
@@ -2592,7 +2650,7 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
       MLevel& f = S->lv[0];
       const size_t words = f.pstride * B;
       const uint32_t n = (uint32_t)f.pstride;
-      const dim3 gu(nblk(n / 4), B), g8(nblk(f.G.csz / 4), B);
+      const dim3 gu(nblk(n / 4), B), g8(rows_blocks(f.G), B);
       float* x = S->xb.p;
       float* p = S->pb.p;
       MK(cudaMemsetAsync(x, 0, words * 4, s));
@@ -2610,13 +2668,12 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
       MK(cudaMemcpyAsync(phi0.p, S->phi.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
       MK(cudaMemcpyAsync(scrB, x, words * 4, cudaMemcpyDeviceToDevice, s));   // x kept
       k_cg_update<false><<<gu, kT, 0, s>>>(x, f.g.p, p, S->qb.p, S->scal.p, f.pstride, n);
-      k_update64_8<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, x, f.G, dm.p, S->fexp.p, f.G.n,
-                                     f.pstride);
+      k_update64<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, x, f.G, dm.p, S->fexp.p, f.G.n,
+                                   f.pstride);
       MK(cudaMemcpyAsync(phi1.p, S->phi.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
       MK(cudaMemcpyAsync(S->phi.p, phi0.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
-      k_update64_8<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, scrB, f.G, dm.p + B, S->fexp.p,
-                                     f.G.n, f.pstride,
-                                     p, S->scal.p);
+      k_update64<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, scrB, f.G, dm.p + B, S->fexp.p,
+                                   f.G.n, f.pstride, p, S->scal.p);
       diff(S->phi.p, phi1.p, 2 * nphi, 5);
       diff(dm.p, dm.p + B, 2 * (size_t)B, 5);
       launches += 6;

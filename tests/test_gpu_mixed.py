@@ -102,6 +102,33 @@ def test_fused_kernels_are_bit_identical(shape, seed):
     assert list(bad) == [0] * 8
 
 
+def test_fixed_point_update_conversion_matches_the_hardware():
+    """The integer-pipe float -> int64 conversion with which the update adds
+    a correction to the fixed-point potential gives the GPU conversion
+    instruction's bits on floats of every exponent: zeros, subnormals,
+    values around one half and the halfway points of every integer step
+    (ties to even both ways), every float with a fraction bit just above or
+    below a half, values at and past 2^63, infinities and NaN."""
+    import ctypes
+    from ion_gym_gb300 import _lib
+    rng = np.random.default_rng(7)
+    random = rng.integers(0, 2 ** 32, 2_000_000, dtype=np.uint64).astype(np.uint32)
+    halves = np.arange(-5000, 5000) + 0.5
+    near = np.concatenate([np.nextafter(halves, np.inf), np.nextafter(halves, -np.inf)])
+    ties = rng.integers(0, 1 << 23, 20_000) + 0.5   # exact in float32
+    special = [0.0, -0.0, 0.5, -0.5, 1.5, 2.5, -2.5, 0.49999997, 2.0 ** 62,
+               2.0 ** 63, -2.0 ** 63, 2.0 ** 64, 1e-45, -1e-45, np.inf, -np.inf,
+               np.nan]
+    floats = np.ascontiguousarray(np.concatenate([
+        np.array(special), halves, near, ties, -ties]).astype(np.float32))
+    floats = np.concatenate([floats, random.view(np.float32)])
+    bad = ctypes.c_longlong(-1)
+    st = _lib.lib().ig_mixed_check_convert(
+        floats.ctypes.data_as(ctypes.c_void_p), floats.size, ctypes.byref(bad))
+    _lib.check(st, "ig_mixed_check_convert")
+    assert bad.value == 0
+
+
 @pytest.mark.parametrize("seed,side,n_el", [(1000, 33, 5), (1001, 65, 12),
                                             (1002, 97, 3), (1003, 65, 16)])
 def test_uneven_batch_decks_reach_fp64_accuracy(seed, side, n_el):
