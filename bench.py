@@ -473,6 +473,7 @@ def rings_measure(a, with_clocks=True):
     by = ctypes.c_double(0)
     L.ig_mixed_time_gs(sess._h, nb, 20, ctypes.byref(ms), ctypes.byref(by))
     achieved = by.value / (ms.value * 1e-3) / 1e9
+    tuning = sess.tuning(nb)
     # e2e through the public API: the session's solve from pinned host masks
     # to pinned host potentials (upload and download inside the timed region)
     masks_h = torch.empty(stack.shape, dtype=torch.uint8).pin_memory().numpy()
@@ -529,6 +530,11 @@ def rings_measure(a, with_clocks=True):
                         "what": "algorithmic bytes of every kernel of every "
                                 "refinement step of the batch over its time"},
         "gpu_launches": int(launches),
+        "smoother_tuning": {**tuning, "what": "the session's tuner on the "
+                            "finest level: the separate half-sweep's launch "
+                            "shape, then passes of 2, 4 and 6 half-sweeps in "
+                            "one temporally blocked launch, the faster per "
+                            "half-sweep taken (the same bits either way)"},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s",
                      "frac": achieved / peak if peak else None,

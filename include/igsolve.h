@@ -225,6 +225,16 @@ int ig_mixed_rebind(void *handle, const uint8_t *metal, long nx, long ny,
  * bytes (6.5 B per node and problem). */
 int ig_mixed_time_gs(void *handle, int n_problems, int pairs,
                      double *ms_per_launch, double *bytes_per_launch);
+/* The smoother shape the session's tuner chose for n_problems problems
+ * (tuning first if it has not run): float4 groups per thread and block
+ * size of the separate half-sweeps; tb[0] = the temporal-block depth taken
+ * for the finest level (half-sweeps per blocked pass; 0 = separate
+ * launches), tb[1] = the fastest blocked depth timed (0 = none timed:
+ * IG_MIXED_TB_LEVELS set, a size-1 axis or a single level); us[0] and
+ * us[1] = their measured microseconds per half-sweep.  No reference
+ * counterpart (a measurement aid). */
+int ig_mixed_tuning(void *handle, int n_problems, int *ng, int *threads,
+                    int tb[2], double us[2]);
 /* Algorithmic DRAM bytes of one refinement step of the session for
  * n_problems problems: every kernel's inputs read once and outputs written
  * once, summed over the captured step (all levels).  A step's time over

@@ -1691,6 +1691,11 @@ std::atomic<long> g_mixed_launches{0};
 struct GsCfg {
   int ng = 1;
   int threads = 256;
+  int tb = 0;  // half-sweeps per temporally blocked pass on the finest level; 0: none
+  // what the tuner measured (us per half-sweep): the chosen separate shape,
+  // and the best blocked depth (0 when none was timed) with its time
+  float sep_us = 0.f, tb_us = 0.f;
+  int tb_best = 0;
 };
 
 // One geometry resident on the device: the FP32 multigrid hierarchy for up
@@ -1745,6 +1750,7 @@ struct Session {
   // one or two CTAs per SM cannot hide), although they move fewer bytes.
   int tb_levels = 0;
   int tb_max = 6;  // half-sweeps per blocked pass (2, 4 or 6); longer phases split
+  bool tb_auto = true;  // the tuner picks tb_levels / tb_max (no environment override)
 
   ~Session() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
@@ -1884,20 +1890,32 @@ struct Session {
     }
   }
 
-  // The smoother's launch shape (groups per thread x block size), timed on
-  // this grid's finest level for nb problems: three red-black pairs per
-  // candidate after one warm pair, the fastest kept.  Shapes are cached per
-  // (grid, problem count) for the process.  Runs before the first graph
-  // capture; the level-0 correction it scribbles on is zeroed before use.
+  // The smoother's launch shape (groups per thread x block size) and its
+  // temporal-block depth, timed on this grid's finest level for nb
+  // problems: three red-black pairs per shape after one warm pair, the
+  // fastest kept; then passes of 2, 4 and 6 half-sweeps in one temporally
+  // blocked launch (k_gs_tb, e into r: two timed after a warm one), taken
+  // for the finest level when one costs less per half-sweep than the best
+  // separate launch.  Either choice gives the same bits.  Shapes are cached
+  // per (grid, problem count) for the process.  Runs before the first graph
+  // capture; the level-0 correction and residual it scribbles on are
+  // rewritten before use.  IG_MIXED_TB_LEVELS, when set, fixes the blocking
+  // instead.
+  void apply_tb(const GsCfg& c) {
+    if (!tb_auto) return;
+    tb_levels = c.tb > 0 ? 1 : 0;
+    if (c.tb > 0) tb_max = c.tb;
+  }
   void tune_gs(int nb) {
     static std::mutex mu;
-    static std::map<std::array<long, 4>, GsCfg> cache;
-    const std::array<long, 4> key{d.nx, d.ny, d.nz, (long)nb};
+    static std::map<std::array<long, 5>, GsCfg> cache;
+    const std::array<long, 5> key{d.nx, d.ny, d.nz, (long)nb, tb_auto ? 1L : 0L};
     {
       std::lock_guard<std::mutex> lk(mu);
       auto it = cache.find(key);
       if (it != cache.end()) {
         gs_cfg = it->second;
+        apply_tb(gs_cfg);
         gs_tuned = true;
         return;
       }
@@ -1927,10 +1945,39 @@ struct Session {
           best = gs_cfg;
         }
       }
+    best.tb = 0;
+    best.sep_us = 1e3f * best_ms / 6.f;
+    if (tb_auto && lv.size() > 1 && !flat(f) && smooth_omega == 1.f) {
+      MK(tb_prepare());
+      float best_per = best_ms / 6.f, tb_per = 1e30f;
+      for (int S2 : {2, 4, 6}) {
+        launch_tb(S2, false, 1, f.e.p, f.r.p, f.g.p, f.mask.p, f.G, f.pstride, nb, s);
+        MK(cudaEventRecord(e0, s));
+        for (int q = 0; q < 2; q++)
+          launch_tb(S2, false, 1, f.e.p, f.r.p, f.g.p, f.mask.p, f.G, f.pstride, nb, s);
+        MK(cudaEventRecord(e1, s));
+        MK(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        MK(cudaEventElapsedTime(&ms, e0, e1));
+        MK(cudaGetLastError());
+        launches += 3;
+        const float per = ms / (2.f * S2);
+        if (per < tb_per) {
+          tb_per = per;
+          best.tb_best = S2;
+          best.tb_us = 1e3f * per;
+        }
+        if (per < best_per) {
+          best_per = per;
+          best.tb = S2;
+        }
+      }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     g_mixed_launches.fetch_add(launches);
     gs_cfg = best;
+    apply_tb(best);
     gs_tuned = true;
     std::lock_guard<std::mutex> lk(mu);
     cache[key] = best;
@@ -2379,7 +2426,10 @@ int open_session(const uint8_t* metal, int nmetal, long nx, long ny, long nz,
     S->cg_iters = std::min(64, std::max(1, cg_iters));
     // IG_MIXED_TB_LEVELS: how many of the finest levels smooth temporally
     // blocked (default 0: separate half-sweeps everywhere)
-    if (const char* v = std::getenv("IG_MIXED_TB_LEVELS")) S->tb_levels = std::max(0, std::atoi(v));
+    if (const char* v = std::getenv("IG_MIXED_TB_LEVELS")) {
+      S->tb_levels = std::max(0, std::atoi(v));
+      S->tb_auto = false;
+    }
     // IG_MIXED_TB_MAX: half-sweeps per blocked pass (2, 4 or 6)
     if (const char* v = std::getenv("IG_MIXED_TB_MAX"))
       S->tb_max = std::min(6, std::max(2, std::atoi(v) & ~1));
@@ -2474,6 +2524,29 @@ int ig_mixed_check_convert(const float* floats, long n, long long* mismatches) {
     MK(cudaMemcpyAsync(&h, mm.p, 8, cudaMemcpyDeviceToHost, s));
     MK(cudaStreamSynchronize(s));
     *mismatches = (long long)h;
+    return IG_OK;
+  } catch (int code) {
+    return code;
+  }
+}
+
+int ig_mixed_tuning(void* handle, int n_problems, int* out_ng, int* out_threads,
+                    int* out_tb, double* out_us) {
+  set_last_error("");
+  Session* S = static_cast<Session*>(handle);
+  if (!S || !out_ng || !out_threads || !out_tb || !out_us || n_problems < 1 ||
+      n_problems > S->bmax) {
+    set_last_error("null argument or problem count outside 1..max_problems");
+    return IG_BAD_ARG;
+  }
+  try {
+    if (!S->gs_tuned) S->tune_gs(n_problems);
+    *out_ng = S->gs_cfg.ng;
+    *out_threads = S->gs_cfg.threads;
+    out_tb[0] = S->gs_cfg.tb;
+    out_tb[1] = S->gs_cfg.tb_best;
+    out_us[0] = S->gs_cfg.sep_us;
+    out_us[1] = S->gs_cfg.tb_us;
     return IG_OK;
   } catch (int code) {
     return code;

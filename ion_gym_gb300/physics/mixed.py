@@ -226,6 +226,23 @@ class MixedSession:
         _lib.check(st, "MixedSession.step_bytes")
         return float(b.value)
 
+    def tuning(self, n_problems=None):
+        """The smoother shape the session's tuner chose (tuning first if
+        needed): {"groups_per_thread", "threads", "temporal_depth" (half-
+        sweeps per blocked pass on the finest level, 0 = separate launches),
+        "us_per_half_sweep", "best_blocked_depth", "blocked_us_per_half_sweep"
+        (the fastest blocked pass timed; 0 and None when none was)}."""
+        ng, th = ctypes.c_int(0), ctypes.c_int(0)
+        tb = (ctypes.c_int * 2)()
+        us = (ctypes.c_double * 2)()
+        n = self.max_problems if n_problems is None else int(n_problems)
+        st = _lib.lib().ig_mixed_tuning(self._h, n, ctypes.byref(ng), ctypes.byref(th), tb, us)
+        _lib.check(st, "MixedSession.tuning")
+        return {"groups_per_thread": ng.value, "threads": th.value,
+                "temporal_depth": tb[0], "us_per_half_sweep": round(us[0], 2),
+                "best_blocked_depth": tb[1],
+                "blocked_us_per_half_sweep": round(us[1], 2) if tb[1] else None}
+
     def _mask_stage(self, B):
         st = getattr(self, "_stage", None)
         if st is None or st.shape[0] < B:

@@ -102,6 +102,34 @@ def test_fused_kernels_are_bit_identical(shape, seed):
     assert list(bad) == [0] * 8
 
 
+def test_tuner_times_launch_shapes_and_temporal_depths():
+    """The session's tuner reports the separate half-sweep shape it chose
+    and the temporal-block depths it timed (2, 4 or 6 half-sweeps per pass
+    on the finest level); whichever it takes, the potentials are those of a
+    session whose blocking is fixed off."""
+    import os
+    from ion_gym_gb300.physics.mixed import MixedSession
+    masks = _deck((41, 37, 45), 1)
+    metal = np.zeros((41, 37, 45), bool)
+    for m in masks.values():
+        metal |= m
+    rings = [masks[i] for i in sorted(masks)]
+    with MixedSession(metal, len(rings)) as s:
+        t = s.tuning()
+        got = s.solve_bases(rings, V, ACC)
+    assert t["groups_per_thread"] in (1, 2, 4, 8) and t["threads"] in (128, 256, 512)
+    assert t["best_blocked_depth"] in (2, 4, 6) and t["temporal_depth"] in (0, 2, 4, 6)
+    assert t["us_per_half_sweep"] > 0 and t["blocked_us_per_half_sweep"] > 0
+    os.environ["IG_MIXED_TB_LEVELS"] = "0"
+    try:
+        with MixedSession(metal, len(rings)) as s:
+            assert s.tuning()["best_blocked_depth"] == 0
+            ref = s.solve_bases(rings, V, ACC)
+    finally:
+        del os.environ["IG_MIXED_TB_LEVELS"]
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+
+
 def test_fixed_point_update_conversion_matches_the_hardware():
     """The integer-pipe float -> int64 conversion with which the update adds
     a correction to the fixed-point potential gives the GPU conversion
