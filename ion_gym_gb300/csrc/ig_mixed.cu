@@ -1263,7 +1263,7 @@ k_update64(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
            const int* __restrict__ fexp, size_t nstride, size_t pstride,
            const float* __restrict__ p = nullptr, const double* __restrict__ scal = nullptr) {
   const uint32_t r = blockIdx.x * kRowWarps + (threadIdx.x >> 5);
-  unsigned long long key = 0;
+  unsigned key32 = 0;
   if (r < (uint32_t)G.nx * (uint32_t)G.ny) {
     const int lane = threadIdx.x & 31;
     const int i = (int)fdivu(r, G.dny);
@@ -1289,13 +1289,14 @@ k_update64(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
       if (p) ev = __fmaf_rn(al, ((k & 1) ? po : pe)[m], ev);
       ev = metal ? 0.f : ev;
       pr[k] = old + f2ll_rn(ev * to_units);
-      unsigned long long kk =
-          static_cast<unsigned long long>(__double_as_longlong(widen(ev))) &
-          0x7fffffffffffffffULL;
-      if (kk > 0x7ff0000000000000ULL) kk = 0x7ff0000000000000ULL;  // NaN: never converged
-      key = max(key, kk);
+      // |ev| as float bits (ordered like the values); NaN counts as
+      // infinity: never converged
+      key32 = max(key32, min(__float_as_uint(ev) & 0x7fffffffu, 0x7f800000u));
     }
   }
+  // the thread's largest |ev| widened once: float64 bits, the same order
+  const unsigned long long key =
+      static_cast<unsigned long long>(__double_as_longlong(widen(__uint_as_float(key32))));
   block_max_to(key, dmax + blockIdx.y);
 }
 
