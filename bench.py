@@ -323,6 +323,7 @@ def run_ours(a):
             gms, gby = _ct.c_double(0), _ct.c_double(0)
             L.ig_mixed_time_gs(sess._h, 1, 20, _ct.byref(gms), _ct.byref(gby))
             gs_gbs = gby.value / (gms.value * 1e-3) / 1e9
+            tuning_m = sess.tuning(1)
             phi_m = np.array(phi_m[0])
         tight = fp64_tight(fixed, val, 2.0)
         line["mixed"] = {
@@ -337,6 +338,7 @@ def run_ours(a):
                               "delta of 1e-13 of the span",
                 "fp64_cascadic_diff_vs_fp64_tight_of_span":
                     float(np.abs(phi64 - tight).max()) / 2.0,
+                "smoother_tuning": tuning_m,
                 "roofline": {"bound": "hbm", "kernel": "k_gs4 (FP32 split "
                              "red-black Gauss-Seidel, 13 B per updated node)",
                              "achieved": gs_gbs, "peak": peak, "unit": "GB/s",

@@ -6,7 +6,8 @@ timing: the arrays are built, a few launches run, the process exits.
 Cases:
   sweep_f64   FP64 red-black sweep (k_sweep<kPlain>) on the 257^3
               quadrupole, `pairs` red-black pairs, omega 1.85
-  mixed       the mixed-precision basis solve of the ring stack (if built)
+  mixed_rings the mixed-precision basis batch of the ring stack (8 bases)
+  mixed_quad  the mixed-precision solve of the 257^3 quadrupole (one problem)
 """
 import argparse
 import ctypes
@@ -73,15 +74,44 @@ def mixed_rings(solves, gs_pairs):
     torch.cuda.synchronize()
 
 
+def mixed_quad(n, solves):
+    """The 257^3 quadrupole (one problem) solved by a resident mixed session
+    to 1e-9 of its 2 V span, `solves` times (values already on the
+    device)."""
+    import torch
+    from ion_gym_gb300 import _lib
+    from ion_gym_gb300.workloads import quadrupole
+    from ion_gym_gb300.physics.mixed import MixedSession
+    fixed, val = quadrupole(n)
+    v = torch.from_numpy(val[None].copy()).cuda()
+    out = torch.empty_like(v)
+    L = _lib.lib()
+    with MixedSession(fixed, 1) as s:
+        for _ in range(solves):
+            steps = ctypes.c_int(0)
+            dmax = np.zeros(1)
+            t0 = time.perf_counter()
+            st = L.ig_mixed_solve_values(s._h, ctypes.c_void_p(v.data_ptr()), 1, 1e-9 * 2.0,
+                                         40, ctypes.c_void_p(out.data_ptr()),
+                                         ctypes.byref(steps),
+                                         dmax.ctypes.data_as(ctypes.c_void_p))
+            _lib.check(st, "mixed_quad")
+            print(f"mixed_quad n={n}: {time.perf_counter() - t0:.4f} s, "
+                  f"{steps.value} refinement steps")
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["sweep_f64", "mixed_rings"])
+    ap.add_argument("case", choices=["sweep_f64", "mixed_rings", "mixed_quad"])
     ap.add_argument("--n", type=int, default=257)
     ap.add_argument("--pairs", type=int, default=4)
     ap.add_argument("--solves", type=int, default=1)
     a = ap.parse_args()
     if a.case == "sweep_f64":
         sweep_f64(a.n, a.pairs)
+    elif a.case == "mixed_quad":
+        mixed_quad(a.n, a.solves)
     else:
         mixed_rings(a.solves, a.pairs)
 
