@@ -495,6 +495,24 @@ def rings_measure(a, with_clocks=True):
     err_door = max(float(np.abs(phi[b] - fp[i]).max()) / V
                    for b, i in enumerate(rings))
     del fp
+    # the field cache's fill (build_stl3d._solve_stl3d_bases: the door, then
+    # unit bases as float32) by the mixed door: unit bases formed on the
+    # device against the float64 potentials converted on the host; each a
+    # whole door call (session build included), after one warm call
+    cache_fill = {}
+    with contextlib.redirect_stdout(sys.stderr):
+        MG.solve_unit_bases_mg(masks, v_basis=V, tol=ACC * V, only=set(rings),
+                               precision="mixed")
+        t = time.perf_counter()
+        MG.solve_unit_bases_mg(masks, v_basis=V, tol=ACC * V, only=set(rings),
+                               precision="mixed")
+        cache_fill["unit_bases_on_device_s"] = time.perf_counter() - t
+        t = time.perf_counter()
+        pm = MG.solve_bases_mg(masks, v_basis=V, tol=ACC * V, only=set(rings),
+                               precision="mixed")
+        {i: (b / V).astype(np.float32) for i, b in pm.items()}
+        cache_fill["host_conversion_s"] = time.perf_counter() - t
+        del pm
     tight = {}
     for b in (0, nb // 2):
         ref = fp64_tight(metal, np.where(masks[rings[b]], V, 0.0), V)
@@ -521,6 +539,11 @@ def rings_measure(a, with_clocks=True):
         "fp64_tight": "drop-in V-cycle (solve3d_vmg) to a cycle delta of "
                       "1e-13 of the span",
         "max_abs_diff_vs_fp64_door_of_span": err_door,
+        "cache_fill": {**cache_fill, "what": "the 8 float32 unit bases of "
+                       "the field cache by the mixed basis door (one call, "
+                       "session build included): converted on the device "
+                       "(solve_unit_bases_mg) against float64 potentials "
+                       "divided and cast on the host"},
         "e2e": {"value": nb * a.steps / el_e2e, "unit": "solves/s",
                 "h2d_bytes_per_step": n * nb,
                 "d2h_bytes_per_step": n * 8 * nb},

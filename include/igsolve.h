@@ -201,6 +201,17 @@ long ig_mixed_bytes_multi(long nx, long ny, long nz, int n_problems);
 int ig_mixed_solve_bases(void *handle, const uint8_t *masks, int n_bases,
                          double v_basis, double acc, int max_steps,
                          double *phi_out, int *steps_out, double *dmax_out);
+/* ig_mixed_solve_bases returning the unit bases the field cache stores
+ * (replaces the host-side (phi / V_BASIS).astype(float32) of
+ * physics/build_stl3d.py:849 after the basis door): unit_out receives
+ * n_bases float32 arrays, each RN32(phi / v_basis) of the float64
+ * potential ig_mixed_solve_bases returns -- the same two roundings, so the
+ * same bits -- formed on the device, so half the bytes come back.  v_basis
+ * must be finite and nonzero. */
+int ig_mixed_solve_unit_bases(void *handle, const uint8_t *masks, int n_bases,
+                              double v_basis, double acc, int max_steps,
+                              float *unit_out, int *steps_out,
+                              double *dmax_out);
 int ig_mixed_solve_values(void *handle, const double *vals, int n_problems,
                           double acc, int max_steps, double *phi_out,
                           int *steps_out, double *dmax_out);

@@ -74,6 +74,7 @@ SIGNATURES = {
     "ig_mixed_open_ex": (_i, [_p, _l, _l, _l, _i, _i, _i, _i, _i, _i, _i,
                               _d, _i, _i, ctypes.POINTER(ctypes.c_void_p)]),
     "ig_mixed_solve_bases": (_i, [_p, _p, _i, _d, _d, _i, _p, _pi, _p]),
+    "ig_mixed_solve_unit_bases": (_i, [_p, _p, _i, _d, _d, _i, _p, _pi, _p]),
     "ig_mixed_solve_values": (_i, [_p, _p, _i, _d, _i, _p, _pi, _p]),
     "ig_mixed_close": (None, [_p]),
     "ig_rasterize": (_i, [_p, _i, _p, _i, _l, _l, _l, _p, _p, _p, _p]),

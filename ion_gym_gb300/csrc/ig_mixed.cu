@@ -1390,6 +1390,23 @@ __global__ void k_fixed_out(long long* __restrict__ phi, const uint8_t* __restri
   reinterpret_cast<double*>(phi)[o] = r;
 }
 
+// The unit bases of a basis solve as float32: RN32(phi / v_basis), phi the
+// float64 potential k_fixed_out would form (v_basis exactly on the basis's
+// own electrode, 0 on the other metal) -- the two roundings of the field
+// cache's (phi / V_BASIS).astype(float32), so the same bits -- into `out`
+// (n floats per problem), for a download of 4 bytes per node instead of 8.
+__global__ void k_unit32_out(const long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
+                             const uint8_t* __restrict__ masks, double v, uint32_t n,
+                             size_t nstride, const int* __restrict__ fexp, float* __restrict__ out) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= n) return;
+  const long long q = phi[blockIdx.y * nstride + t];
+  const uint8_t metal = fixed[t];
+  double r = __ll2double_rn(q) * pow2d(fexp[blockIdx.y] - 56);
+  if (metal) r = masks[(size_t)blockIdx.y * n + t] ? v : 0.0;
+  out[(size_t)blockIdx.y * n + t] = __double2float_rn(__ddiv_rn(r, v));
+}
+
 // f2ll_rn against the hardware conversion: mism counts the inputs whose
 // results differ.
 __global__ void k_check_convert(const float* __restrict__ fv, uint32_t n,
@@ -2377,13 +2394,25 @@ void set_units(Session& S, const std::vector<double>& vmax) {
 // The float64 potentials (Dirichlet values exact at the metal: vals, or
 // v_basis on the basis masks) into phi_out.
 int finish(Session& S, const MixedResult& r, double* phi_out, int* steps_out,
-           double* dmax_out, const double* vals, const uint8_t* masks, double v) {
+           double* dmax_out, const double* vals, const uint8_t* masks, double v,
+           float* unit_out = nullptr) {
   g_mixed_launches.fetch_add(S.launches_per_step() * r.steps + 1);
   const uint32_t n = (uint32_t)S.d.n();
-  k_fixed_out<<<dim3(nblk(n), S.B), kT, 0, S.s>>>(S.phi.p, S.fixed.p, vals, masks, v, n, n,
-                                                  S.fexp.p, S.lv[0].G.mnat);
-  MK(cudaGetLastError());
-  MK(cudaMemcpyAsync(phi_out, S.phi.p, S.d.n() * S.B * 8, cudaMemcpyDefault, S.s));
+  if (unit_out) {
+    // float32 unit bases, staged in the finest level's correction buffer
+    // (scratch once the refinement is done; it holds pstride >= n floats
+    // per problem)
+    float* u = S.lv[0].e.p;
+    k_unit32_out<<<dim3(nblk(n), S.B), kT, 0, S.s>>>(S.phi.p, S.fixed.p, masks, v, n, n,
+                                                     S.fexp.p, u);
+    MK(cudaGetLastError());
+    MK(cudaMemcpyAsync(unit_out, u, (size_t)n * S.B * 4, cudaMemcpyDefault, S.s));
+  } else {
+    k_fixed_out<<<dim3(nblk(n), S.B), kT, 0, S.s>>>(S.phi.p, S.fixed.p, vals, masks, v, n, n,
+                                                    S.fexp.p, S.lv[0].G.mnat);
+    MK(cudaGetLastError());
+    MK(cudaMemcpyAsync(phi_out, S.phi.p, S.d.n() * S.B * 8, cudaMemcpyDefault, S.s));
+  }
   MK(cudaStreamSynchronize(S.s));
   if (steps_out) *steps_out = r.steps;
   if (dmax_out) std::memcpy(dmax_out, r.dmax.data(), 8 * S.B);
@@ -2797,13 +2826,21 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
   }
 }
 
-int ig_mixed_solve_bases(void* handle, const uint8_t* masks, int n_bases,
-                         double v_basis, double acc, int max_steps,
-                         double* phi_out, int* steps_out, double* dmax_out) {
+}  // extern "C"
+
+namespace {
+// The basis solve behind ig_mixed_solve_bases (phi_out) and
+// ig_mixed_solve_unit_bases (unit_out).
+int solve_bases_to(Session* S, const uint8_t* masks, int n_bases, double v_basis, double acc,
+                   int max_steps, double* phi_out, float* unit_out, int* steps_out,
+                   double* dmax_out) {
   set_last_error("");
-  Session* S = static_cast<Session*>(handle);
-  if (!S || !masks || !phi_out || n_bases < 1 || n_bases > S->bmax) {
+  if (!S || !masks || !(phi_out || unit_out) || n_bases < 1 || n_bases > S->bmax) {
     set_last_error("null argument or basis count outside 1..max_problems");
+    return IG_BAD_ARG;
+  }
+  if (unit_out && !(std::fabs(v_basis) > 0.0 && std::isfinite(v_basis))) {
+    set_last_error("ig_mixed_solve_unit_bases: v_basis must be finite and nonzero");
     return IG_BAD_ARG;
   }
   if (S->nmetal > 1) {
@@ -2826,10 +2863,35 @@ int ig_mixed_solve_bases(void* handle, const uint8_t* masks, int n_bases,
     MK(cudaGetLastError());
     const std::vector<double> accs(n_bases, acc);
     const MixedResult r = run_mixed(*S, accs.data(), max_steps);
-    return finish(*S, r, phi_out, steps_out, dmax_out, nullptr, S->stage.p, v_basis);
+    return finish(*S, r, phi_out, steps_out, dmax_out, nullptr, S->stage.p, v_basis, unit_out);
   } catch (int code) {
     return code;
   }
+}
+}  // namespace
+
+extern "C" {
+
+int ig_mixed_solve_bases(void* handle, const uint8_t* masks, int n_bases,
+                         double v_basis, double acc, int max_steps,
+                         double* phi_out, int* steps_out, double* dmax_out) {
+  if (!phi_out) {
+    set_last_error("null argument or basis count outside 1..max_problems");
+    return IG_BAD_ARG;
+  }
+  return solve_bases_to(static_cast<Session*>(handle), masks, n_bases, v_basis, acc,
+                        max_steps, phi_out, nullptr, steps_out, dmax_out);
+}
+
+int ig_mixed_solve_unit_bases(void* handle, const uint8_t* masks, int n_bases,
+                              double v_basis, double acc, int max_steps, float* unit_out,
+                              int* steps_out, double* dmax_out) {
+  if (!unit_out) {
+    set_last_error("null argument or basis count outside 1..max_problems");
+    return IG_BAD_ARG;
+  }
+  return solve_bases_to(static_cast<Session*>(handle), masks, n_bases, v_basis, acc,
+                        max_steps, nullptr, unit_out, steps_out, dmax_out);
 }
 
 int ig_mixed_solve_values(void* handle, const double* vals, int n_problems,

@@ -155,13 +155,15 @@ def solve_stl3d_bases(masks, mirror_axes=(False, False, False),
     basis door at V_BASIS and STL3D_SOLVE_TOL, returned as float32 unit
     bases.  precision (not in the reference signature): None / "fp64" runs
     the reference's V-cycle (its bits), "mixed" the batched mixed-precision
-    session to the same tolerance; solve_code.solve_code_key(precision)
+    session to the same tolerance, its unit bases formed on the device
+    (multigrid3d.solve_unit_bases_mg); solve_code.solve_code_key(precision)
     keys the cache entry on the choice."""
-    from ion_gym_gb300.physics.multigrid3d import solve_bases_mg
-    bases = solve_bases_mg(masks, mirror=mirror_axes, v_basis=V_BASIS,
-                           tol=STL3D_SOLVE_TOL, stencil="ghost_linear",
-                           verbose=verbose, precision=precision)
-    return {i: (b / V_BASIS).astype(np.float32) for i, b in bases.items()}
+    from ion_gym_gb300.physics.multigrid3d import solve_unit_bases_mg
+    # mirror_axes only shapes theta, which the STL route does not build
+    # (theta None), as in the reference
+    return solve_unit_bases_mg(masks, v_basis=V_BASIS, tol=STL3D_SOLVE_TOL,
+                               stencil="ghost_linear", verbose=verbose,
+                               precision=precision)
 
 
 def store_bases(spec, bases, masks, root=None):

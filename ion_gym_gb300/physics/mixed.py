@@ -119,6 +119,18 @@ class MixedSession:
         potentials (B, nx, ny, nz) float64: a new numpy array, or `out` (a
         C-contiguous float64 numpy array -- pinned for a fast download -- or
         CUDA tensor) when given."""
+        return self._bases(masks, v_basis, accuracy, max_steps, out, np.float64)
+
+    def solve_unit_bases(self, masks, v_basis=1e4, accuracy=1e-9, max_steps=40,
+                         out=None):
+        """solve_bases returning the unit bases the field cache stores:
+        float32 (B, nx, ny, nz), each (phi / v_basis).astype(float32) of the
+        float64 potential solve_bases returns, bit for bit, formed on the
+        device (half the bytes to download).  `out`: a C-contiguous float32
+        numpy array or CUDA tensor to fill."""
+        return self._bases(masks, v_basis, accuracy, max_steps, out, np.float32)
+
+    def _bases(self, masks, v_basis, accuracy, max_steps, out, dtype):
         if type(masks).__module__.startswith("torch"):
             B = int(masks.shape[0])
             mptr = ctypes.c_void_p(masks.data_ptr())
@@ -136,13 +148,14 @@ class MixedSession:
                 stack[b] = np.asarray(m, bool)
             mptr = ptr(stack)
         if out is None:
-            phi = np.empty((B,) + self.shape)
+            phi = np.empty((B,) + self.shape, dtype)
             pptr = ptr(phi)
         elif isinstance(out, np.ndarray):
-            if out.dtype != np.float64 or not out.flags.c_contiguous or \
+            if out.dtype != dtype or not out.flags.c_contiguous or \
                     out.shape != (B,) + self.shape:
-                raise ValueError("solve_bases: out must be a C-contiguous float64 "
-                                 f"array of shape {(B,) + self.shape}")
+                raise ValueError(f"solve_bases: out must be a C-contiguous "
+                                 f"{np.dtype(dtype).name} array of shape "
+                                 f"{(B,) + self.shape}")
             phi = out
             pptr = ptr(out)
         else:
@@ -151,9 +164,10 @@ class MixedSession:
         steps = ctypes.c_int(0)
         dmax = np.zeros(B)
         span = abs(float(v_basis))
-        st = _lib.lib().ig_mixed_solve_bases(
-            self._h, mptr, B, float(v_basis), float(accuracy) * span,
-            int(max_steps), pptr, ctypes.byref(steps), ptr(dmax))
+        fn = (_lib.lib().ig_mixed_solve_bases if dtype == np.float64
+              else _lib.lib().ig_mixed_solve_unit_bases)
+        st = fn(self._h, mptr, B, float(v_basis), float(accuracy) * span,
+                int(max_steps), pptr, ctypes.byref(steps), ptr(dmax))
         self._outcome(st, steps.value, dmax, accuracy, span)
         self.last_steps = int(steps.value)
         return phi
@@ -286,9 +300,11 @@ def max_batch(shape, n_bases, budget_frac=0.8):
 
 def solve_bases_mixed(masks, v_basis=1e4, accuracy=1e-9,
                       stencil="ghost_linear", only=None, max_steps=40,
-                      return_stats=False, batch=None, on_batch=None, **cycle):
+                      return_stats=False, batch=None, on_batch=None, unit=False,
+                      **cycle):
     """All bases of a deck by the mixed-precision session: {index: mask} ->
-    {index: phi float64 at v_basis}.  The bases run in batches of `batch`
+    {index: phi float64 at v_basis} (unit: {index: (phi / v_basis) as
+    float32}, formed on the device, MixedSession.solve_unit_bases).  The bases run in batches of `batch`
     (default: as many as free device memory holds, all of them when they
     fit) on one resident session.  on_batch(done, total, indices), when
     given, is called before each batch (and may raise to stop).  With
@@ -310,8 +326,8 @@ def solve_bases_mixed(masks, v_basis=1e4, accuracy=1e-9,
             part = items[q:q + B]
             if on_batch is not None:
                 on_batch(q, len(items), [i for i, _ in part])
-            phi = s.solve_bases([m for _, m in part], v_basis, accuracy,
-                                max_steps)
+            solve = s.solve_unit_bases if unit else s.solve_bases
+            phi = solve([m for _, m in part], v_basis, accuracy, max_steps)
             out.update({i: phi[b] for b, (i, _) in enumerate(part)})
             steps = max(steps, s.last_steps)
             nb += 1

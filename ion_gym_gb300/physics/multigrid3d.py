@@ -288,11 +288,12 @@ def basis_precision(precision=None):
     return p
 
 
-def _solve_bases_mixed_door(masks, todo, v_basis, tol, stencil, verbose):
+def _solve_bases_mixed_door(masks, todo, v_basis, tol, stencil, verbose, unit=False):
     """The basis door's mixed-precision form: every requested basis in
     batched mixed-precision sessions, each to tol volts (tol / |v_basis|
     of the electrode span, in the max norm against the converged FP64
-    solution of the same discrete problem)."""
+    solution of the same discrete problem).  unit: float32 unit bases
+    (phi / v_basis) formed on the device instead of float64 potentials."""
     from ion_gym_gb300.physics.mixed import solve_bases_mixed
     n = len(masks)
     want = {i for _, i, _ in todo}
@@ -310,7 +311,7 @@ def _solve_bases_mixed_door(masks, todo, v_basis, tol, stencil, verbose):
     out, st = solve_bases_mixed(masks, v_basis=v_basis,
                                 accuracy=float(tol) / abs(float(v_basis)),
                                 stencil=stencil, only=want, return_stats=True,
-                                on_batch=progress)
+                                on_batch=progress, unit=unit)
     secs = time.time() - t0
     print(f"  {len(out)} bases in {st['batches']} mixed-precision batch(es), "
           f"{st['steps']} refinement steps ({secs:.1f}s)", flush=True)
@@ -318,6 +319,28 @@ def _solve_bases_mixed_door(masks, todo, v_basis, tol, stencil, verbose):
     for _ in out:
         _record_solve(int(np.prod(shape)), secs / max(len(out), 1))
     return {i: out[i] for _, i, _ in todo}
+
+
+def solve_unit_bases_mg(masks, v_basis=1e4, tol=1e-6, verbose=False,
+                        stencil="ghost_linear", only=None, precision=None):
+    """The basis door followed by the field cache's conversion to unit
+    bases, {index: (phi / v_basis).astype(float32)} (build_stl3d.py:835-849:
+    _solve_stl3d_bases divides the door's potentials by V_BASIS and stores
+    float32).  With precision "mixed" the division and the cast run on the
+    device after the batched solve (the same two roundings, so the same
+    bits as converting solve_bases_mg's result on the host) and half the
+    bytes come back; "fp64" converts the bit-exact door's result on the
+    host.  Theta None only (the cache's STL route has no scene)."""
+    prec = basis_precision(precision)
+    if prec == "mixed":
+        stencil_code(stencil)
+        todo = [(j, i, m) for j, (i, m) in enumerate(sorted(masks.items()), 1)
+                if only is None or i in only]
+        return _solve_bases_mixed_door(masks, todo, v_basis, tol, stencil,
+                                       verbose, unit=True)
+    bases = solve_bases_mg(masks, v_basis=v_basis, tol=tol, verbose=verbose,
+                           stencil=stencil, only=only, precision=prec)
+    return {i: (b / v_basis).astype(np.float32) for i, b in bases.items()}
 
 
 def solve_bases_mg(masks, scene=None, mirror=(False, False, False),

@@ -202,6 +202,12 @@ def test_solve_stl3d_bases_golden_and_mixed(M, drivers_golden):
     for i in (1, 2, 3):
         assert mixed[i].dtype == np.float32
         assert np.abs(mixed[i].astype(np.float64) - got[i]).max() <= 2e-8 + 2.0 ** -23
+    # the mixed route forms the unit bases on the device: the bits of the
+    # host conversion of the same session's float64 potentials
+    phi = M.solve_bases_mg(masks, v_basis=1e4, tol=1e-4, precision="mixed")
+    for i in (1, 2, 3):
+        want = (phi[i] / 1e4).astype(np.float32)
+        assert np.array_equal(mixed[i].view(np.uint32), want.view(np.uint32))
 
 
 def test_basis_door_mixed_precision_batches(M):
