@@ -470,7 +470,7 @@ def rings_measure(a, with_clocks=True):
     launches = L.ig_launch_count() + _mixed_launches(L) - launches0
     phi = out.cpu().numpy()
     steps_per_solve = sess.last_steps
-    batch_bytes = steps_per_solve * sess.step_bytes(nb)
+    batch_bytes = sess.solve_bytes()
     ms = ctypes.c_double(0)
     by = ctypes.c_double(0)
     L.ig_mixed_time_gs(sess._h, nb, 20, ctypes.byref(ms), ctypes.byref(by))
@@ -664,7 +664,7 @@ def run_uneven(a):
             else:
                 s.rebind(fixed)
             s.solve_values(val, 1e-9, out=out, span=span)
-            return [s.last_steps], s.last_steps * s.step_bytes(1)
+            return [s.last_steps], s.solve_bytes()
         units = order
     else:
         groups = {}
@@ -693,7 +693,7 @@ def run_uneven(a):
             else:
                 s.rebind(fixed)
             s.solve_values(val, 1e-9, out=out, span=spans)
-            return [s.last_steps] * len(spans), s.last_steps * s.step_bytes(len(spans))
+            return [s.last_steps] * len(spans), s.solve_bytes()
         opened = sessions
         units = order
 
@@ -741,7 +741,7 @@ def run_uneven(a):
                 ctypes.c_void_p(odev[k].data_ptr()), ctypes.byref(st_),
                 dm.ctypes.data_as(ctypes.c_void_p))
             _lib.check(rc, "uneven resident solve")
-            return st_.value * s.step_bytes(len(qs))
+            return s.solve_bytes()
 
         with cf.ThreadPoolExecutor(workers) as ex:
             list(ex.map(solve_res, range(len(res))))

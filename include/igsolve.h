@@ -252,6 +252,10 @@ int ig_mixed_tuning(void *handle, int n_problems, int *ng, int *threads,
  * this gives the whole step's achieved bandwidth.  No reference
  * counterpart (a measurement aid). */
 int ig_mixed_step_bytes(void *handle, int n_problems, double *bytes_out);
+/* The algorithmic bytes of every refinement step of the session's last
+ * solve (ig_mixed_step_bytes times its steps).  No reference counterpart
+ * (a measurement aid). */
+int ig_mixed_solve_bytes(void *handle, double *bytes_out);
 /* Checks the integer-pipe float -> int64 conversion (round to nearest
  * even) that the mixed path's update uses to add a correction to the
  * fixed-point potential against the GPU's own conversion instruction, bit

@@ -992,11 +992,16 @@ k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
       const int ca = (xi[a] + yi[b] + m0) & 1;
       const float* A = eb + (size_t)ca * C.csz + row;
       const float* Bc = eb + (size_t)(1 - ca) * C.csz + row;
+      // slots (m0 >> 1) and the next of both colours as 8-byte loads (the
+      // row offset is even: H and m0 >> 1 are), in bounds even where they
+      // lie past the row's last node (padding), which the guards zero
+      const float2 a01 = *reinterpret_cast<const float2*>(A);
+      const float2 b01 = *reinterpret_cast<const float2*>(Bc);
       float cv[5];
-      cv[0] = A[0];
-      cv[1] = m0 + 1 < C.nz ? Bc[0] : 0.f;
-      cv[2] = m0 + 2 < C.nz ? A[1] : 0.f;
-      cv[3] = m0 + 3 < C.nz ? Bc[1] : 0.f;
+      cv[0] = a01.x;
+      cv[1] = m0 + 1 < C.nz ? b01.x : 0.f;
+      cv[2] = m0 + 2 < C.nz ? a01.y : 0.f;
+      cv[3] = m0 + 3 < C.nz ? b01.y : 0.f;
       cv[4] = m0 + 4 < C.nz ? A[2] : 0.f;
       const float w = xw[a] * yw[b];
 #pragma unroll
@@ -1799,6 +1804,7 @@ struct Session {
   int tb_levels = 0;
   int tb_max = 6;  // half-sweeps per blocked pass (2, 4 or 6); longer phases split
   bool tb_auto = true;  // the tuner picks tb_levels / tb_max (no environment override)
+  double last_solve_bytes = 0.0;  // algorithmic bytes of the last solve's steps
 
   ~Session() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
@@ -2323,6 +2329,8 @@ struct MixedResult {
   int status;
   int steps;
   std::vector<double> dmax;
+  long launches;  // kernel launches of the steps
+  double bytes;   // algorithmic bytes of the steps
 };
 
 // Refinement steps until every problem is within acc of its converged
@@ -2340,9 +2348,11 @@ MixedResult run_mixed(Session& M, const double* acc, int max_steps) {
   if (M.method == 1) M.cg_init();
   std::vector<unsigned long long> h(M.B);
   std::vector<double> prev(M.B, INFINITY), prev_rho(M.B, 0.0);
-  MixedResult res{IG_NOT_CONVERGED, 0, std::vector<double>(M.B, 0.0)};
+  MixedResult res{IG_NOT_CONVERGED, 0, std::vector<double>(M.B, 0.0), 0, 0.0};
   for (int it = 0; it < max_steps; it++) {
     M.step();
+    res.launches += M.launches_per_step();
+    res.bytes += M.step_bytes(M.B);
     MK(cudaMemcpyAsync(h.data(), M.dmax.p, 8 * M.B, cudaMemcpyDeviceToHost, M.s));
     MK(cudaStreamSynchronize(M.s));
     res.steps = it + 1;
@@ -2362,6 +2372,7 @@ MixedResult run_mixed(Session& M, const double* acc, int max_steps) {
       break;
     }
   }
+  M.last_solve_bytes = res.bytes;
   return res;
 }
 
@@ -2396,7 +2407,7 @@ void set_units(Session& S, const std::vector<double>& vmax) {
 int finish(Session& S, const MixedResult& r, double* phi_out, int* steps_out,
            double* dmax_out, const double* vals, const uint8_t* masks, double v,
            float* unit_out = nullptr) {
-  g_mixed_launches.fetch_add(S.launches_per_step() * r.steps + 1);
+  g_mixed_launches.fetch_add(r.launches + 1);
   const uint32_t n = (uint32_t)S.d.n();
   if (unit_out) {
     // float32 unit bases, staged in the finest level's correction buffer
@@ -2615,6 +2626,17 @@ int ig_mixed_tuning(void* handle, int n_problems, int* out_ng, int* out_threads,
   } catch (int code) {
     return code;
   }
+}
+
+int ig_mixed_solve_bytes(void* handle, double* bytes_out) {
+  set_last_error("");
+  Session* S = static_cast<Session*>(handle);
+  if (!S || !bytes_out) {
+    set_last_error("null argument");
+    return IG_BAD_ARG;
+  }
+  *bytes_out = S->last_solve_bytes;
+  return IG_OK;
 }
 
 int ig_mixed_step_bytes(void* handle, int n_problems, double* bytes_out) {

@@ -240,6 +240,14 @@ class MixedSession:
         _lib.check(st, "MixedSession.step_bytes")
         return float(b.value)
 
+    def solve_bytes(self):
+        """Algorithmic DRAM bytes of every refinement step of the last
+        solve."""
+        b = ctypes.c_double(0.0)
+        _lib.check(_lib.lib().ig_mixed_solve_bytes(self._h, ctypes.byref(b)),
+                   "MixedSession.solve_bytes")
+        return float(b.value)
+
     def tuning(self, n_problems=None):
         """The smoother shape the session's tuner chose (tuning first if
         needed): {"groups_per_thread", "threads", "temporal_depth" (half-

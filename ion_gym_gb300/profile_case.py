@@ -8,6 +8,7 @@ Cases:
               quadrupole, `pairs` red-black pairs, omega 1.85
   mixed_rings the mixed-precision basis batch of the ring stack (8 bases)
   mixed_quad  the mixed-precision solve of the 257^3 quadrupole (one problem)
+  mixed_board the mixed-precision bases of a 512x128x96 planar board
 """
 import argparse
 import ctypes
@@ -101,9 +102,34 @@ def mixed_quad(n, solves):
     torch.cuda.synchronize()
 
 
+def mixed_board(solves, n_el=24):
+    """A seeded 512x128x96 planar board (n_el extruded electrodes on two
+    layers plus the grounded box): its unit bases in one resident session
+    to 1e-9 of the span, `solves` times (masks already on the device)."""
+    import torch
+    from ion_gym_gb300.workloads import planar_board
+    from ion_gym_gb300.physics.mixed import MixedSession
+    masks, box = planar_board(101, shape=(512, 128, 96), n_electrodes=n_el)
+    masks = {k: m for k, m in masks.items() if m.any()}
+    metal = box.copy()
+    for m in masks.values():
+        metal |= m
+    stack = torch.from_numpy(
+        np.stack([masks[k] for k in sorted(masks)]).view(np.uint8)).cuda()
+    out = torch.empty(stack.shape, dtype=torch.float64, device="cuda")
+    with MixedSession(metal, len(masks)) as s:
+        for _ in range(solves):
+            t0 = time.perf_counter()
+            s.solve_bases(stack, 1e4, 1e-9, out=out)
+            print(f"mixed_board: {len(masks)} bases in {time.perf_counter() - t0:.4f} s, "
+                  f"{s.last_steps} refinement steps")
+    torch.cuda.synchronize()
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["sweep_f64", "mixed_rings", "mixed_quad"])
+    ap.add_argument("case", choices=["sweep_f64", "mixed_rings", "mixed_quad",
+                                     "mixed_board"])
     ap.add_argument("--n", type=int, default=257)
     ap.add_argument("--pairs", type=int, default=4)
     ap.add_argument("--solves", type=int, default=1)
@@ -112,6 +138,8 @@ def main():
         sweep_f64(a.n, a.pairs)
     elif a.case == "mixed_quad":
         mixed_quad(a.n, a.solves)
+    elif a.case == "mixed_board":
+        mixed_board(a.solves)
     else:
         mixed_rings(a.solves, a.pairs)
 

@@ -117,6 +117,7 @@ def test_tuner_times_launch_shapes_and_temporal_depths():
     with MixedSession(metal, len(rings)) as s:
         t = s.tuning()
         got = s.solve_bases(rings, V, ACC)
+        assert s.solve_bytes() == s.last_steps * s.step_bytes(len(rings)) > 0
     assert t["groups_per_thread"] in (1, 2, 4, 8) and t["threads"] in (128, 256, 512)
     assert t["best_blocked_depth"] in (2, 4, 6) and t["temporal_depth"] in (0, 2, 4, 6)
     assert t["us_per_half_sweep"] > 0 and t["blocked_us_per_half_sweep"] > 0
