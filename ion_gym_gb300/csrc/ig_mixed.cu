@@ -1255,6 +1255,62 @@ k_resid64(const long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
   }
 }
 
+// k_resid64 for short rows: a warp takes R consecutive natural rows as one
+// run of R * nz nodes (each lane's row and k from one division, its plane
+// and row-in-plane from another), so a warp has enough of the row's steps
+// in flight even when nz is small; the same expressions per node.
+__global__ void __launch_bounds__(kT)
+k_resid64_flat(const long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
+               SGeo G, float* __restrict__ g, const int* __restrict__ fexp, float nscale,
+               size_t nstride, size_t pstride, uint32_t R) {
+  const uint32_t nrows = (uint32_t)G.nx * (uint32_t)G.ny;
+  const uint32_t r0 = (blockIdx.x * kRowWarps + (threadIdx.x >> 5)) * R;
+  if (r0 >= nrows) return;  // whole warps
+  const uint32_t lane = threadIdx.x & 31;
+  const int nz = G.nz;
+  const uint32_t span = min(R, nrows - r0) * (uint32_t)nz;
+  const long long* p = phi + blockIdx.y * nstride;
+  const uint8_t* fb = fixed + (size_t)blockIdx.y * G.mnat;
+  float* gb = g + blockIdx.y * pstride;
+  const float u = pow2f(fexp[blockIdx.y] - 56);
+#pragma unroll 4
+  for (uint32_t q = lane; q < span; q += 32) {
+    const uint32_t rr = fdivu(q, G.dnz);
+    const int k = (int)(q - rr * (uint32_t)nz);
+    const uint32_t r = r0 + rr;
+    const int i = (int)fdivu(r, G.dny);
+    const int j = (int)(r - (uint32_t)i * G.dny.d);
+    const size_t o = (size_t)r * nz;
+    const int km = k > 0 ? k - 1 : (nz > 1 ? 1 : k);
+    const int kp = k + 1 < nz ? k + 1 : (nz > 1 ? nz - 2 : k);
+    const uint8_t metal = fb[o + k];
+    const long long s =
+        ((p[((size_t)lo_i(i, G.nx) * G.ny + j) * nz + k] +
+          p[((size_t)hi_i(i, G.nx) * G.ny + j) * nz + k]) +
+         (p[((size_t)i * G.ny + lo_i(j, G.ny)) * nz + k] +
+          p[((size_t)i * G.ny + hi_i(j, G.ny)) * nz + k])) +
+        (p[o + km] + p[o + kp]);
+    const long long c = p[o + k];
+    const long long rv = s - ((c << 2) + (c << 1));
+    gb[(size_t)((i + j + k) & 1) * G.csz + (size_t)r * G.H + (k >> 1)] =
+        metal ? 0.f : __ll2float_rn(rv) * u * nscale;
+  }
+}
+
+// Natural rows per warp for the residual and the update: 1 (one warp per
+// row, k_resid64 / k_update64) when rows are long enough to keep a warp's
+// loads in flight, else enough rows for about 256 nodes (the _flat forms).
+// force: -1 the rule, 0 always one row per warp, 1 always several.
+inline uint32_t flat_rows(const SGeo& G, int force) {
+  if (force == 0) return 1;
+  if (force == 1) return (uint32_t)std::max(2, (256 + G.nz - 1) / G.nz);
+  return G.nz >= 192 ? 1u : (uint32_t)std::max(2, (256 + G.nz - 1) / G.nz);
+}
+inline unsigned flat_blocks(const SGeo& G, uint32_t R) {
+  const size_t warps = ((size_t)G.nx * G.ny + R - 1) / R;
+  return (unsigned)((warps + kRowWarps - 1) / kRowWarps);
+}
+
 // float -> double by its bits for zeros and normal floats (exponent rebias,
 // significand moved up 29 bits); subnormals, infinities and NaN convert on
 // the FP64 pipe.
@@ -1326,6 +1382,52 @@ k_update64(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
   // the warp's largest |ev| (float bits order like the values), widened
   // once to float64 bits; a warp whose maximum beats the stored one raises
   // it -- no block barrier, so a warp leaves as soon as its row is done
+  const unsigned wmax = __reduce_max_sync(0xffffffffu, key32);
+  if ((threadIdx.x & 31) == 0 && wmax) {
+    const unsigned long long key =
+        static_cast<unsigned long long>(__double_as_longlong(widen(__uint_as_float(wmax))));
+    if (key > *reinterpret_cast<volatile unsigned long long*>(dmax + blockIdx.y))
+      atomicMax(dmax + blockIdx.y, key);
+  }
+}
+
+// k_update64 for short rows: R consecutive natural rows per warp as one run
+// (see k_resid64_flat); the same expressions per node.
+__global__ void __launch_bounds__(kT)
+k_update64_flat(long long* __restrict__ phi, const uint8_t* __restrict__ fixed,
+                const float* __restrict__ e, SGeo G, unsigned long long* dmax,
+                const int* __restrict__ fexp, size_t nstride, size_t pstride,
+                const float* __restrict__ p, const double* __restrict__ scal, uint32_t R) {
+  const uint32_t nrows = (uint32_t)G.nx * (uint32_t)G.ny;
+  const uint32_t r0 = (blockIdx.x * kRowWarps + (threadIdx.x >> 5)) * R;
+  unsigned key32 = 0;
+  if (r0 < nrows) {
+    const uint32_t lane = threadIdx.x & 31;
+    const int nz = G.nz;
+    const uint32_t span = min(R, nrows - r0) * (uint32_t)nz;
+    long long* P = phi + blockIdx.y * nstride + (size_t)r0 * nz;
+    const uint8_t* F = fixed + (size_t)blockIdx.y * G.mnat + (size_t)r0 * nz;
+    const size_t pb = blockIdx.y * pstride;
+    const float al = p ? (float)scal[4 * blockIdx.y + 1] : 0.f;
+    const float to_units = pow2f(56 - fexp[blockIdx.y]);
+#pragma unroll 2
+    for (uint32_t q = lane; q < span; q += 32) {
+      const uint32_t rr = fdivu(q, G.dnz);
+      const int k = (int)(q - rr * (uint32_t)nz);
+      const uint32_t r = r0 + rr;
+      const int i = (int)fdivu(r, G.dny);
+      const int j = (int)(r - (uint32_t)i * G.dny.d);
+      const size_t so = pb + (size_t)((i + j + k) & 1) * G.csz + (size_t)r * G.H + (k >> 1);
+      const uint8_t metal = F[q];
+      const long long old = P[q];
+      float ev = e ? e[so] : 0.f;
+      if (p) ev = __fmaf_rn(al, p[so], ev);
+      ev = metal ? 0.f : ev;
+      const long long nv = old + f2ll_rn(ev * to_units);
+      if (!metal) P[q] = nv;
+      key32 = max(key32, min(__float_as_uint(ev) & 0x7fffffffu, 0x7f800000u));
+    }
+  }
   const unsigned wmax = __reduce_max_sync(0xffffffffu, key32);
   if ((threadIdx.x & 31) == 0 && wmax) {
     const unsigned long long key =
@@ -1805,6 +1907,7 @@ struct Session {
   int tb_max = 6;  // half-sweeps per blocked pass (2, 4 or 6); longer phases split
   bool tb_auto = true;  // the tuner picks tb_levels / tb_max (no environment override)
   double last_solve_bytes = 0.0;  // algorithmic bytes of the last solve's steps
+  int rows_force = -1;  // rows per warp of the residual and update: -1 by rule (flat_rows)
 
   ~Session() {
     for (auto& g : graphs) cudaGraphExecDestroy(g.second);
@@ -2146,25 +2249,43 @@ struct Session {
       for (int c = 1; c >= 0; c--) launch_gs(a, c, B, smooth_omega);
   }
 
+  // the finest level's FP64 residual and potential update, one warp per
+  // natural row or, for short rows, several rows per warp (flat_rows)
+  void launch_resid64() {
+    MLevel& f = lv[0];
+    const uint32_t R = flat_rows(f.G, rows_force);
+    if (R == 1)
+      k_resid64<<<dim3(rows_blocks(f.G), B), kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, fexp.p,
+                                                         (float)-resid_scale, f.G.n, f.pstride);
+    else
+      k_resid64_flat<<<dim3(flat_blocks(f.G, R), B), kT, 0, s>>>(
+          phi.p, fixed.p, f.G, f.g.p, fexp.p, (float)-resid_scale, f.G.n, f.pstride, R);
+  }
+  void launch_update64(const float* e, unsigned long long* dm, const float* p,
+                       const double* sc) {
+    MLevel& f = lv[0];
+    const uint32_t R = flat_rows(f.G, rows_force);
+    if (R == 1)
+      k_update64<<<dim3(rows_blocks(f.G), B), kT, 0, s>>>(phi.p, fixed.p, e, f.G, dm, fexp.p,
+                                                          f.G.n, f.pstride, p, sc);
+    else
+      k_update64_flat<<<dim3(flat_blocks(f.G, R), B), kT, 0, s>>>(
+          phi.p, fixed.p, e, f.G, dm, fexp.p, f.G.n, f.pstride, p, sc, R);
+  }
+
   // one refinement step: FP64 residual, V-cycles on the correction, update
   void step_enqueue() {
     MLevel& f = lv[0];
-    const size_t nstride = f.G.n;
-    const dim3 gn(rows_blocks(f.G), B);
-    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, fexp.p, (float)-resid_scale, nstride,
-                                f.pstride);
+    launch_resid64();
     for (int v = 0; v < vcycles; v++) vcycle(0, v == 0);
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
-    k_update64<<<dim3(rows_blocks(f.G), B), kT, 0, s>>>(phi.p, fixed.p, f.e.p, f.G, dmax.p,
-                                                         fexp.p, nstride, f.pstride);
+    launch_update64(f.e.p, dmax.p, nullptr, nullptr);
   }
 
   // the flexible CG: once per solve, the FP64 residual and zero state
   void cg_init() {
     MLevel& f = lv[0];
-    const dim3 gn(rows_blocks(f.G), B);
-    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, fexp.p, (float)-resid_scale, f.G.n,
-                                f.pstride);
+    launch_resid64();
     MK(cudaMemsetAsync(xb.p, 0, f.pstride * B * 4, s));
     MK(cudaMemsetAsync(pb.p, 0, f.pstride * B * 4, s));
     p_in_b2 = false;
@@ -2206,14 +2327,10 @@ struct Session {
         k_cg_update<false><<<dim3(nblk(n / 4), B), kT, 0, s>>>(xb.p, f.g.p, pcur, qb.p, scal.p,
                                                               f.pstride, n);
     }
-    const dim3 gn(rows_blocks(f.G), B);
     MK(cudaMemsetAsync(dmax.p, 0, 8 * B, s));
     // phi += x + alpha p (x absent when the step has one iteration)
-    k_update64<<<dim3(rows_blocks(f.G), B), kT, 0, s>>>(
-        phi.p, fixed.p, cg_iters > 1 ? xb.p : nullptr, f.G, dmax.p, fexp.p, f.G.n, f.pstride,
-        pcur, scal.p);
-    k_resid64<<<gn, kT, 0, s>>>(phi.p, fixed.p, f.G, f.g.p, fexp.p, (float)-resid_scale, f.G.n,
-                                f.pstride);
+    launch_update64(cg_iters > 1 ? xb.p : nullptr, dmax.p, pcur, scal.p);
+    launch_resid64();
   }
 
   // a step ends with the direction in the other buffer when the fused CG
@@ -2501,6 +2618,9 @@ int open_session(const uint8_t* metal, int nmetal, long nx, long ny, long nz,
     S->cg_iters = std::min(64, std::max(1, cg_iters));
     // IG_MIXED_TB_LEVELS: how many of the finest levels smooth temporally
     // blocked (default 0: separate half-sweeps everywhere)
+    // IG_MIXED_FLAT: 0 = one natural row per warp in the FP64 residual and
+    // update, 1 = several rows per warp, unset = by row length
+    if (const char* v = std::getenv("IG_MIXED_FLAT")) S->rows_force = std::atoi(v) ? 1 : 0;
     if (const char* v = std::getenv("IG_MIXED_TB_LEVELS")) {
       S->tb_levels = std::max(0, std::atoi(v));
       S->tb_auto = false;
@@ -2697,6 +2817,7 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
   try {
     if (!S->gs_tuned) S->tune_gs(n_problems);
     const int B = n_problems;
+    S->B = B;  // the session's launch helpers run B problems (each solve sets it anew)
     cudaStream_t s = S->s;
     Buf<unsigned long long> bad;
     bad.alloc(8, s);
@@ -2809,7 +2930,7 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
       MLevel& f = S->lv[0];
       const size_t words = f.pstride * B;
       const uint32_t n = (uint32_t)f.pstride;
-      const dim3 gu(nblk(n / 4), B), g8(rows_blocks(f.G), B);
+      const dim3 gu(nblk(n / 4), B);
       float* x = S->xb.p;
       float* p = S->pb.p;
       MK(cudaMemsetAsync(x, 0, words * 4, s));
@@ -2827,12 +2948,10 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
       MK(cudaMemcpyAsync(phi0.p, S->phi.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
       MK(cudaMemcpyAsync(scrB, x, words * 4, cudaMemcpyDeviceToDevice, s));   // x kept
       k_cg_update<false><<<gu, kT, 0, s>>>(x, f.g.p, p, S->qb.p, S->scal.p, f.pstride, n);
-      k_update64<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, x, f.G, dm.p, S->fexp.p, f.G.n,
-                                   f.pstride);
+      S->launch_update64(x, dm.p, nullptr, nullptr);
       MK(cudaMemcpyAsync(phi1.p, S->phi.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
       MK(cudaMemcpyAsync(S->phi.p, phi0.p, nphi * 8, cudaMemcpyDeviceToDevice, s));
-      k_update64<<<g8, kT, 0, s>>>(S->phi.p, S->fixed.p, scrB, f.G, dm.p + B, S->fexp.p,
-                                   f.G.n, f.pstride, p, S->scal.p);
+      S->launch_update64(scrB, dm.p + B, p, S->scal.p);
       diff(S->phi.p, phi1.p, 2 * nphi, 5);
       diff(dm.p, dm.p + B, 2 * (size_t)B, 5);
       launches += 6;

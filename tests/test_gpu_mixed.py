@@ -131,6 +131,29 @@ def test_tuner_times_launch_shapes_and_temporal_depths():
     assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
 
 
+@pytest.mark.parametrize("shape", [(41, 37, 45), (30, 20, 200)])
+def test_row_and_flat_residual_update_give_the_same_bits(shape):
+    """The FP64 residual and update run one natural row per warp or several
+    rows per warp (short rows); both forms give the same potentials, bit
+    for bit (a short-row grid and one past the switch)."""
+    import os
+    from ion_gym_gb300.physics.mixed import MixedSession
+    masks = _deck(shape, 3)
+    metal = np.zeros(shape, bool)
+    for m in masks.values():
+        metal |= m
+    rings = [masks[i] for i in sorted(masks)]
+    got = {}
+    for force in ("0", "1"):
+        os.environ["IG_MIXED_FLAT"] = force
+        try:
+            with MixedSession(metal, len(rings)) as s:
+                got[force] = s.solve_bases(rings, V, ACC)
+        finally:
+            del os.environ["IG_MIXED_FLAT"]
+    assert np.array_equal(got["0"].view(np.uint64), got["1"].view(np.uint64))
+
+
 def test_fixed_point_update_conversion_matches_the_hardware():
     """The integer-pipe float -> int64 conversion with which the update adds
     a correction to the fixed-point potential gives the GPU conversion
