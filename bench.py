@@ -16,8 +16,8 @@ Prints one JSON line.  `value` is solves/s with the inputs resident in HBM;
 `e2e` is the same solve through the public API from pinned host buffers
 (host->device copies of mask and Dirichlet values, device->host copy of phi
 inside the timed region).  The line also carries the same quadrupole through
-the mixed-precision session (`mixed`), the ring-stack basis batch of BASELINE
-config 3 (`rings`: mixed against the FP64 drop-in basis door) and one
+the mixed-precision session (`mixed`), the 8-basis ring-stack batch
+(`rings`: mixed against the FP64 drop-in basis door) and one
 complete CPU solve (`cpu_baseline`).  `--impl reference` times the oracle's
 restatement of the reference's CPU path (oracle/, all host threads), each
 step one complete solve of the same workload.
@@ -424,7 +424,7 @@ def _mixed_launches(L):
 
 
 def rings_measure(a, with_clocks=True):
-    """Batched ring-stack bases (BASELINE config 3): the 8 unit bases of a
+    """Batched ring-stack bases: the 8 unit bases of a
     seeded ring stack (193x193x385, grounded box) in one batch, mixed
     precision to 1e-9 of the span, against the FP64 drop-in basis door (the
     reference's V-cycle at tol = 1e-9 x span, bit-identical to the
@@ -598,7 +598,7 @@ def run_rings(a):
 
 
 def run_uneven(a):
-    """Uneven batch (BASELINE config 4): 64 seeded geometries, cubic sides
+    """Uneven batch: 64 seeded geometries, cubic sides
     from {33,65,97,129,193,257}, 2-16 random electrodes at U(-100,100) V,
     each solved to 1e-9 of its own span by the mixed path.  One step = the
     whole batch of 64; every upload, mask build, solve and download is
@@ -912,10 +912,10 @@ def serve_rate(srv, pool, rate, duration, max_requests, fresh, ring_frac,
 
 
 def run_serve(a):
-    """Served load (BASELINE config 5): Poisson arrivals of basis-solve
+    """Served load: Poisson arrivals of basis-solve
     requests -- planar boards up to 512x128x96 with 8-32 extruded
-    electrodes on two layers plus the grounded box, and ring-stack decks of
-    config 3 -- through serve.FieldServer (continuous batching, resident
+    electrodes on two layers plus the grounded box, and 193x193x385
+    ring-stack decks -- through serve.FieldServer (continuous batching, resident
     geometries, HBM admission, bases kept in HBM); a fraction of the
     requests are fresh geometries.  Swept over the offered rates `--rates`,
     p50/p99 latency beside throughput per rate; `value` is the highest
@@ -1159,7 +1159,7 @@ def main():
     ap.add_argument("--fresh", type=float, default=0.1,
                     help="serve: fraction of requests with a new geometry")
     ap.add_argument("--ring-frac", type=float, default=0.2,
-                    help="serve: fraction of ring-stack (config 3) decks")
+                    help="serve: fraction of ring-stack (193x193x385, 8 rings) decks")
     ap.add_argument("--workers", type=int, default=4)
     ap.add_argument("--uneven-mode", default="shape", choices=["shape", "deck"],
                     help="uneven: decks of one grid shape as one batch, or one by one")

@@ -1168,8 +1168,8 @@ __global__ void k_split_mask(const uint8_t* __restrict__ nat, SGeo G, uint8_t* _
 // in magnitude and the int64 range leaves 128x headroom.  One unit is
 // 2^-56 of the largest value: finer than a float64 ulp there (2^-53).
 // Benefits: the reference's fine residual sum(nbr) - 6 phi is an exact
-// integer sum (the float64 values of the round-1 form had to be aligned to
-// a common exponent first, about 130 integer operations per node); the
+// integer sum (an earlier float64 form had to align the values to a common
+// exponent first, about 130 integer operations per node); the
 // update adds the rounded correction; the float64 potential is formed once,
 // at the end, with the Dirichlet values written exactly at the metal.
 

@@ -16,8 +16,8 @@ there; the same kernels are pinned to it bit for bit on smaller grids):
   V-cycle run to 1e-13 of the span, and one basis matches the FP64 drop-in
   basis door (tol 1e-9 of the span) to the door's own accuracy.
 
-The mixed path's tolerance is the spec accuracy, 1e-9 of the span, in
-the max norm over every node.
+The mixed path's tolerance is its stated accuracy, 1e-9 of the span, in the
+max norm over every node.
 """
 import numpy as np
 import pytest
