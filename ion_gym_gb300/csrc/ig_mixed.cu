@@ -300,20 +300,16 @@ __device__ __forceinline__ float4 zero_start_e0(const float* gp, const uint8_t* 
                      zero_start_e0(g.w, m.w));
 }
 
-__global__ void __launch_bounds__(kT)
-k_gs_zero_pair(float* __restrict__ e, const float* __restrict__ g,
-               const uint8_t* __restrict__ mask, SGeo G, size_t pstride) {
-  mask += (size_t)blockIdx.y * G.msplit;
-  const uint32_t t = blockIdx.x * kT + threadIdx.x;
-  if (t >= (G.csz >> 2)) return;
+// Float4 group t (both colours) of the fused first pair, for one problem:
+// e0, g0 and mask its split arrays (colour 1 at + csz).
+__device__ __forceinline__ void zero_pair_at(float* e0, const float* g0, const uint8_t* mask,
+                                             const SGeo& G, uint32_t t) {
   const uint32_t ij = fdivu(t, G.dH4);
   const int m0 = 4 * (int)(t - ij * G.dH4.d);
   const int i = (int)fdivu(ij, G.dny);
   const int j = (int)(ij - (uint32_t)i * G.dny.d);
   const uint32_t base = ij * (uint32_t)G.H + m0;
-  float* e0 = e + blockIdx.y * pstride;
   float* e1 = e0 + G.csz;
-  const float* g0 = g + blockIdx.y * pstride;
   const float* g1 = g0 + G.csz;
   const uint8_t* k0 = mask;
   const uint8_t* k1 = mask + G.csz;
@@ -352,6 +348,15 @@ k_gs_zero_pair(float* __restrict__ e, const float* __restrict__ g,
     o[u] = mv[u] ? 0.f : (q - gv[u]) * (1.0f / 6.0f);
   }
   *reinterpret_cast<float4*>(e1 + base) = make_float4(o[0], o[1], o[2], o[3]);
+}
+
+__global__ void __launch_bounds__(kT)
+k_gs_zero_pair(float* __restrict__ e, const float* __restrict__ g,
+               const uint8_t* __restrict__ mask, SGeo G, size_t pstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= (G.csz >> 2)) return;
+  zero_pair_at(e + blockIdx.y * pstride, g + blockIdx.y * pstride,
+               mask + (size_t)blockIdx.y * G.msplit, G, t);
 }
 
 // ---- temporal blocking: S red-black half-sweeps in one pass -----------------
@@ -623,26 +628,23 @@ k_resid0(const float* __restrict__ e, const float* __restrict__ g,
 // k_resid0 over float4 groups (grids with no size-1 axis): the same
 // expressions per slot, 16-byte loads of the colour-1 neighbour rows, one
 // float4 store of r.
-__global__ void __launch_bounds__(kT)
-k_resid0_4(const float* __restrict__ e, const float* __restrict__ g,
-           const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ r,
-           size_t pstride) {
-  mask += (size_t)blockIdx.y * G.msplit;
-  const uint32_t t = blockIdx.x * kT + threadIdx.x;
-  if (t >= (G.csz >> 2)) return;
+// Float4 group t of the colour-0 residual, one problem: eb, gb, mask its
+// split arrays, rb its colour-0 residual (csz floats).
+__device__ __forceinline__ void resid0_4_at(const float* eb, const float* gb,
+                                            const uint8_t* mask, const SGeo& G, float* rb,
+                                            uint32_t t) {
   const uint32_t ij = fdivu(t, G.dH4);
   const int m0 = 4 * (int)(t - ij * G.dH4.d);
   const int i = (int)fdivu(ij, G.dny);
   const int j = (int)(ij - (uint32_t)i * G.dny.d);
   const uint32_t base = ij * (uint32_t)G.H + m0;
-  float4* out = reinterpret_cast<float4*>(r + blockIdx.y * (size_t)G.csz + base);
+  float4* out = reinterpret_cast<float4*>(rb + base);
   // no early exit on an all-metal group: the loads are in bounds in every
   // group and go out with the mask's; metal slots select 0 below
   const uchar4 mk = *reinterpret_cast<const uchar4*>(mask + base);
-  const float* eb = e + blockIdx.y * pstride;
   float q[4];
   nbr4(PlainLd{eb + G.csz}, G, i, j, m0, (i + j) & 1, base, q);
-  const float4 ev = ld4(eb + base), gg = ld4(g + blockIdx.y * pstride + base);
+  const float4 ev = ld4(eb + base), gg = ld4(gb + base);
   const float es[4] = {ev.x, ev.y, ev.z, ev.w}, gv[4] = {gg.x, gg.y, gg.z, gg.w};
   const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
   float o[4];
@@ -652,6 +654,16 @@ k_resid0_4(const float* __restrict__ e, const float* __restrict__ g,
     o[u] = mv[u] ? 0.f : gv[u] - a;
   }
   *out = make_float4(o[0], o[1], o[2], o[3]);
+}
+
+__global__ void __launch_bounds__(kT)
+k_resid0_4(const float* __restrict__ e, const float* __restrict__ g,
+           const uint8_t* __restrict__ mask, SGeo G, float* __restrict__ r,
+           size_t pstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= (G.csz >> 2)) return;
+  resid0_4_at(e + blockIdx.y * pstride, g + blockIdx.y * pstride,
+              mask + (size_t)blockIdx.y * G.msplit, G, r + blockIdx.y * (size_t)G.csz, t);
 }
 
 // 4 x full weighting when only colour 0 of the fine residual is nonzero:
@@ -723,18 +735,16 @@ __device__ __forceinline__ float restrict0_node(const float* __restrict__ rb, co
 // (di, dj, dk) order with its weights, so the bits are the same; groups
 // that touch a face use that loop per node.  The four results go to the
 // coarse split layout as two 8-byte stores (kc alternates colour).
-__global__ void __launch_bounds__(kT)
-k_restrict0_4(const float* __restrict__ r0, SGeo F, float* __restrict__ gc, SGeo C,
-              size_t cstride) {
+// Coarse nodes 4t' .. of the four-node restriction, one problem: rb its
+// fine colour-0 residual, gb its coarse right-hand side (split layout);
+// t < C.nx * C.ny * ((C.nz + 3) / 4).
+__device__ __forceinline__ void restrict0_4_at(const float* rb, const SGeo& F, float* gb,
+                                               const SGeo& C, uint32_t t) {
   const uint32_t G4 = (uint32_t)(C.nz + 3) >> 2;
-  const uint32_t t = blockIdx.x * kT + threadIdx.x;
-  if (t >= (uint32_t)C.nx * C.ny * G4) return;
   const uint32_t ij = t / G4;
   const int kc0 = 4 * (int)(t - ij * G4);
   const int ic = (int)fdivu(ij, C.dny);
   const int jc = (int)(ij - (uint32_t)ic * C.dny.d);
-  const float* rb = r0 + blockIdx.y * (size_t)F.csz;
-  float* gb = gc + blockIdx.y * cstride;
   const bool inner = ic >= 1 && 2 * ic + 1 <= F.nx - 1 && jc >= 1 && 2 * jc + 1 <= F.ny - 1 &&
                      kc0 >= 1 && 2 * (kc0 + 3) + 1 <= F.nz - 1;
   if (!inner) {
@@ -787,6 +797,14 @@ k_restrict0_4(const float* __restrict__ r0, SGeo F, float* __restrict__ gc, SGeo
   *reinterpret_cast<float2*>(gb + (size_t)ca * C.csz + cs) = make_float2(0.5f * a[0], 0.5f * a[2]);
   *reinterpret_cast<float2*>(gb + (size_t)(1 - ca) * C.csz + cs) =
       make_float2(0.5f * a[1], 0.5f * a[3]);
+}
+
+__global__ void __launch_bounds__(kT)
+k_restrict0_4(const float* __restrict__ r0, SGeo F, float* __restrict__ gc, SGeo C,
+              size_t cstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= (uint32_t)C.nx * C.ny * ((uint32_t)(C.nz + 3) >> 2)) return;
+  restrict0_4_at(r0 + blockIdx.y * (size_t)F.csz, F, gc + blockIdx.y * cstride, C, t);
 }
 
 // r = g - A e on natural layout (0 at metal).
@@ -942,14 +960,12 @@ k_prolong_add4_gather(const float* __restrict__ ec, SGeo C, float* __restrict__ 
 // skipped zero weights and the x, y, z summation order are those of
 // k_prolong_add4_gather, so the results are the same bits.  Needs every
 // axis of both grids at least 2 nodes long.
-__global__ void __launch_bounds__(kT)
-k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
-               const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
-               size_t fstride) {
-  maskf += (size_t)blockIdx.y * F.msplit;
-  const int c = blockIdx.z;  // gridDim.z = 1: colour 0 only
-  const uint32_t t = blockIdx.x * kT + threadIdx.x;
-  if (t >= (F.csz >> 2)) return;
+// Fine float4 group t of colour c of the windowed prolongation, one
+// problem: eb its coarse correction, efb its fine correction and maskf its
+// fine split mask.
+__device__ __forceinline__ void prolong_add4_at(const float* eb, const SGeo& C, float* efb,
+                                                const uint8_t* maskf, const SGeo& F, int c,
+                                                uint32_t t) {
   const uint32_t ij = fdivu(t, F.dH4);
   const int m0 = 4 * (int)(t - ij * F.dH4.d);
   const int i = (int)fdivu(ij, F.dny);
@@ -960,7 +976,6 @@ k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
   // all-metal (or unused) group skips only the read-modify-write below
   const uchar4 mk = *reinterpret_cast<const uchar4*>(maskf + (size_t)c * F.csz + base);
   const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
-  const float* eb = ec + blockIdx.y * cstride;
   const LerpF x = pa(i, C.nx), y = pa(j, C.ny);
   // the nonzero x (y) weights in order: a0 with 1 - t unless t = 1, then a1
   // with t unless t = 0 (t is 0, 1/2 or 1)
@@ -1013,7 +1028,7 @@ k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
       }
     }
   if (mk.x & mk.y & mk.z & mk.w) return;  // metal or unused: nothing to add
-  float4* out = reinterpret_cast<float4*>(ef + fstride * blockIdx.y + (size_t)c * F.csz + base);
+  float4* out = reinterpret_cast<float4*>(efb + (size_t)c * F.csz + base);
   float4 v = *out;
   v.x += mv[0] ? 0.f : acc[0];
   v.y += mv[1] ? 0.f : acc[1];
@@ -1022,17 +1037,23 @@ k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
   *out = v;
 }
 
-// Coarsest level: red-black SOR in shared memory, one CTA per problem, a
-// fixed number of pairs (the level has at most kBottomMax nodes).
-__global__ void __launch_bounds__(kBottomThreads)
-k_bottom(float* __restrict__ e, const float* __restrict__ g,
-         const uint8_t* __restrict__ mask, SGeo G, float omega, int pairs,
-         size_t pstride) {
-  mask += (size_t)blockIdx.x * G.msplit;
-  __shared__ float se[kBottomMax];
-  __shared__ float sg[kBottomMax];
-  float* eb = e + blockIdx.x * pstride;
-  const float* gb = g + blockIdx.x * pstride;
+__global__ void __launch_bounds__(kT)
+k_prolong_add4(const float* __restrict__ ec, SGeo C, float* __restrict__ ef,
+               const uint8_t* __restrict__ maskf, SGeo F, size_t cstride,
+               size_t fstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= (F.csz >> 2)) return;
+  prolong_add4_at(ec + blockIdx.y * cstride, C, ef + fstride * blockIdx.y,
+                  maskf + (size_t)blockIdx.y * F.msplit, F, blockIdx.z, t);
+}
+
+// The coarsest level's SOR pairs for one problem, by the calling CTA
+// (kBottomThreads threads, all of which must call it): eb (out), gb and
+// mask the problem's split arrays, se and sg shared scratch of kBottomMax
+// floats each.
+__device__ __forceinline__ void bottom_at(float* eb, const float* gb, const uint8_t* mask,
+                                          const SGeo& G, float omega, int pairs, float* se,
+                                          float* sg) {
   // A thread's nodes (at most kBottomMax / kBottomThreads): their colour,
   // whether they are free, and their six neighbours' slots, worked out once
   // so that the pairs below run on shared memory alone.
@@ -1087,6 +1108,99 @@ k_bottom(float* __restrict__ e, const float* __restrict__ g,
     }
   }
 }
+
+// Coarsest level: red-black SOR in shared memory, one CTA per problem, a
+// fixed number of pairs (the level has at most kBottomMax nodes).
+__global__ void __launch_bounds__(kBottomThreads)
+k_bottom(float* __restrict__ e, const float* __restrict__ g,
+         const uint8_t* __restrict__ mask, SGeo G, float omega, int pairs,
+         size_t pstride) {
+  __shared__ float se[kBottomMax];
+  __shared__ float sg[kBottomMax];
+  bottom_at(e + blockIdx.x * pstride, g + blockIdx.x * pstride,
+            mask + (size_t)blockIdx.x * G.msplit, G, omega, pairs, se, sg);
+}
+
+// The cycle of the level just above the bottom, the bottom solve included,
+// by one CTA per problem in shared memory: the level's right-hand side and
+// masks are read once and its correction written once, so the dozen
+// launches of a few blocks that the separate kernels take on these small
+// grids -- each a few microseconds of latency -- become one.  The phases
+// are the device code of those kernels (zero_pair_at, gs4_group,
+// resid0_4_at, restrict0_4_at, bottom_at, prolong_add4_at) over the CTA's
+// threads, in their order, so the result has their bits.  Shared memory:
+// the bottom's scratch (2 kBottomMax floats), the level's correction and
+// right-hand side (2 csz floats each), its colour-0 residual (csz floats),
+// the bottom's correction and right-hand side (2 csz_b floats each), then
+// both masks (2 csz + 2 csz_b bytes); tail_smem_bytes() gives the total.
+__global__ void __launch_bounds__(kBottomThreads)
+k_tail_cycle(float* __restrict__ e, const float* __restrict__ g,
+             const uint8_t* __restrict__ mask, SGeo A, size_t apstride,
+             const uint8_t* __restrict__ bmask, SGeo Bt, int nu1, int nu2, float omega_b,
+             int pairs) {
+  extern __shared__ float4 tail_smem[];
+  float* se = reinterpret_cast<float*>(tail_smem);
+  float* sg = se + kBottomMax;
+  float* ae = sg + kBottomMax;
+  float* ag = ae + 2 * (size_t)A.csz;
+  float* ar = ag + 2 * (size_t)A.csz;
+  float* be = ar + (size_t)A.csz;
+  float* bg = be + 2 * (size_t)Bt.csz;
+  uint8_t* am = reinterpret_cast<uint8_t*>(bg + 2 * (size_t)Bt.csz);
+  uint8_t* bm = am + 2 * (size_t)A.csz;
+  const uint32_t tid = threadIdx.x;
+  const float* gA = g + blockIdx.x * apstride;
+  const uint8_t* mA = mask + (size_t)blockIdx.x * A.msplit;
+  const uint8_t* mB = bmask + (size_t)blockIdx.x * Bt.msplit;
+  const uint32_t na4 = (2 * A.csz) >> 2, nb4 = (2 * Bt.csz) >> 2;
+  for (uint32_t q = tid; q < na4; q += kBottomThreads) {
+    reinterpret_cast<float4*>(ag)[q] = ld4(gA + 4 * (size_t)q);
+    reinterpret_cast<uchar4*>(am)[q] = reinterpret_cast<const uchar4*>(mA)[q];
+  }
+  for (uint32_t q = tid; q < nb4; q += kBottomThreads)
+    reinterpret_cast<uchar4*>(bm)[q] = reinterpret_cast<const uchar4*>(mB)[q];
+  __syncthreads();
+  const uint32_t nq = A.csz >> 2;
+  // pre-smoothing: the fused first pair from e = 0, then nu1 - 1 pairs
+  for (uint32_t t = tid; t < nq; t += kBottomThreads) zero_pair_at(ae, ag, am, A, t);
+  __syncthreads();
+  for (int q = 1; q < nu1; q++)
+    for (int c = 0; c < 2; c++) {
+      for (uint32_t t = tid; t < nq; t += kBottomThreads)
+        gs4_group<false>(ae + (size_t)c * A.csz, ae + (size_t)(1 - c) * A.csz,
+                         ag + (size_t)c * A.csz, am + (size_t)c * A.csz, A, c, 1.f, t);
+      __syncthreads();
+    }
+  // the colour-0 residual, restricted to the bottom's right-hand side
+  for (uint32_t t = tid; t < nq; t += kBottomThreads) resid0_4_at(ae, ag, am, A, ar, t);
+  __syncthreads();
+  const uint32_t nr = (uint32_t)Bt.nx * Bt.ny * ((uint32_t)(Bt.nz + 3) >> 2);
+  for (uint32_t t = tid; t < nr; t += kBottomThreads) restrict0_4_at(ar, A, bg, Bt, t);
+  __syncthreads();
+  bottom_at(be, bg, bm, Bt, omega_b, pairs, se, sg);
+  __syncthreads();
+  // colour 0 takes the prolonged correction (the first post-smoothing
+  // half-sweep, colour 1, rewrites every free colour-1 slot)
+  for (uint32_t t = tid; t < nq; t += kBottomThreads) prolong_add4_at(be, Bt, ae, am, A, 0, t);
+  __syncthreads();
+  for (int q = 0; q < nu2; q++)
+    for (int c = 1; c >= 0; c--) {
+      for (uint32_t t = tid; t < nq; t += kBottomThreads)
+        gs4_group<false>(ae + (size_t)c * A.csz, ae + (size_t)(1 - c) * A.csz,
+                         ag + (size_t)c * A.csz, am + (size_t)c * A.csz, A, c, 1.f, t);
+      __syncthreads();
+    }
+  float* eA = e + blockIdx.x * apstride;
+  for (uint32_t q = tid; q < na4; q += kBottomThreads)
+    reinterpret_cast<float4*>(eA)[q] = reinterpret_cast<const float4*>(ae)[q];
+}
+
+// Shared bytes k_tail_cycle needs for level A above the bottom Bt.
+inline size_t tail_smem_bytes(const SGeo& A, const SGeo& Bt) {
+  return 4 * (2 * (size_t)kBottomMax + 5 * (size_t)A.csz + 4 * (size_t)Bt.csz) +
+         2 * (size_t)A.csz + 2 * (size_t)Bt.csz;
+}
+constexpr size_t kTailSmemMax = 200 * 1024;
 
 // Coarse metal of the FP32 correction's hierarchy: injection with a rescue
 // of thin metal.  Coarse node (i, j, k) is metal when fine node
@@ -1906,6 +2020,8 @@ struct Session {
   int tb_levels = 0;
   int tb_max = 6;  // half-sweeps per blocked pass (2, 4 or 6); longer phases split
   bool tb_auto = true;  // the tuner picks tb_levels / tb_max (no environment override)
+  bool tail_on = true;   // k_tail_cycle allowed (IG_MIXED_TAIL=0: the separate launches)
+  bool tail_ok = false;  // ... and usable on this hierarchy
   double last_solve_bytes = 0.0;  // algorithmic bytes of the last solve's steps
   int rows_force = -1;  // rows per warp of the residual and update: -1 by rule (flat_rows)
 
@@ -1996,6 +2112,18 @@ struct Session {
     }
     load_metal(metal);
     bottom_omega = (float)omega_of(lv.back().d);
+    // the level just above the bottom cycles in one CTA per problem
+    // (k_tail_cycle) when its arrays fit in shared memory
+    tail_ok = false;
+    if (tail_on && lv.size() >= 2) {
+      const MLevel& ta = lv[lv.size() - 2];
+      const MLevel& tb = lv.back();
+      tail_ok = !flat(ta) && two_or_more(ta) && two_or_more(tb) && smooth_omega == 1.f &&
+                nu1 >= 1 && nu2 >= 1 && tail_smem_bytes(ta.G, tb.G) <= kTailSmemMax;
+      if (tail_ok)
+        MK(cudaFuncSetAttribute(k_tail_cycle, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kTailSmemMax));
+    }
     if (tb_levels > 0) MK(tb_prepare());
     phi.alloc(n * bmax, s);
     fexp.alloc(bmax, s);
@@ -2162,6 +2290,10 @@ struct Session {
   bool fuse_dir() const { return pb2.p != nullptr; }
 
   // The first pre-smoothing pair from e = 0 runs as one fused pass.
+  // level l's cycle from zero runs as k_tail_cycle (l the last level above
+  // the bottom, no temporal blocking there)
+  bool tail_level(size_t l) const { return tail_ok && l + 2 == lv.size() && !use_tb(l); }
+
   bool fuse_zero_pair(const MLevel& a) const {
     return nu1 >= 1 && smooth_omega == 1.f && !flat(a);
   }
@@ -2180,6 +2312,13 @@ struct Session {
     if (l + 1 == lv.size()) {
       k_bottom<<<B, kBottomThreads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, bottom_omega,
                                             bottom_pairs, a.pstride);
+      return;
+    }
+    if (zero && tail_level(l)) {
+      const MLevel& b = lv[l + 1];
+      k_tail_cycle<<<B, kBottomThreads, tail_smem_bytes(a.G, b.G), s>>>(
+          a.e.p, a.g.p, a.mask.p, a.G, a.pstride, b.mask.p, b.G, nu1, nu2, bottom_omega,
+          bottom_pairs);
       return;
     }
     int q0 = 0;
@@ -2367,6 +2506,7 @@ struct Session {
 
   long cycle_launches(size_t l, bool zero) const {
     if (l + 1 == lv.size()) return 1;
+    if (zero && tail_level(l)) return 1;
     const int reps = coarse_visits(l);
     long n = 3;                                         // residual, restriction, prolongation
     if (tb_pre(l, zero)) n += tb_passes(2 * nu1);
@@ -2383,6 +2523,8 @@ struct Session {
     const MLevel& a = lv[l];
     const double n = (double)a.G.n;
     if (l + 1 == lv.size()) return 9.0 * n;            // g, mask in; e out
+    // k_tail_cycle: g and mask in, e out, the bottom's mask in
+    if (zero && tail_level(l)) return 9.0 * n + (double)lv[l + 1].G.n;
     double b = 0.0;
     int q0 = 0;
     if (tb_pre(l, zero)) {
@@ -2621,6 +2763,8 @@ int open_session(const uint8_t* metal, int nmetal, long nx, long ny, long nz,
     // IG_MIXED_FLAT: 0 = one natural row per warp in the FP64 residual and
     // update, 1 = several rows per warp, unset = by row length
     if (const char* v = std::getenv("IG_MIXED_FLAT")) S->rows_force = std::atoi(v) ? 1 : 0;
+    // IG_MIXED_TAIL=0: the last level above the bottom by separate launches
+    if (const char* v = std::getenv("IG_MIXED_TAIL")) S->tail_on = std::atoi(v) != 0;
     if (const char* v = std::getenv("IG_MIXED_TB_LEVELS")) {
       S->tb_levels = std::max(0, std::atoi(v));
       S->tb_auto = false;

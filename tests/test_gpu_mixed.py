@@ -154,6 +154,30 @@ def test_row_and_flat_residual_update_give_the_same_bits(shape):
     assert np.array_equal(got["0"].view(np.uint64), got["1"].view(np.uint64))
 
 
+@pytest.mark.parametrize("shape,n_b", [((41, 37, 45), 4), ((64, 48, 40), 1),
+                                       ((70, 66, 34), 3)])
+def test_tail_cycle_gives_the_separate_launches_bits(shape, n_b):
+    """The cycle of the level above the bottom in one CTA per problem
+    (k_tail_cycle) gives the potentials of the separate launches, bit for
+    bit: odd and even extents, one problem and batches."""
+    import os
+    from ion_gym_gb300.physics.mixed import MixedSession
+    masks = _deck(shape, 4)
+    metal = np.zeros(shape, bool)
+    for m in masks.values():
+        metal |= m
+    rings = [masks[i] for i in sorted(masks)][:n_b]
+    got = {}
+    for tail in ("0", "1"):
+        os.environ["IG_MIXED_TAIL"] = tail
+        try:
+            with MixedSession(metal, len(rings)) as s:
+                got[tail] = s.solve_bases(rings, V, ACC)
+        finally:
+            del os.environ["IG_MIXED_TAIL"]
+    assert np.array_equal(got["0"].view(np.uint64), got["1"].view(np.uint64))
+
+
 def test_fixed_point_update_conversion_matches_the_hardware():
     """The integer-pipe float -> int64 conversion with which the update adds
     a correction to the fixed-point potential gives the GPU conversion
