@@ -2758,13 +2758,13 @@ int open_session(const uint8_t* metal, int nmetal, long nx, long ny, long nz,
     S->smooth_omega = (float)std::min(1.9, std::max(0.5, smooth_omega));
     S->method = method == 0 ? 0 : 1;
     S->cg_iters = std::min(64, std::max(1, cg_iters));
-    // IG_MIXED_TB_LEVELS: how many of the finest levels smooth temporally
-    // blocked (default 0: separate half-sweeps everywhere)
     // IG_MIXED_FLAT: 0 = one natural row per warp in the FP64 residual and
     // update, 1 = several rows per warp, unset = by row length
     if (const char* v = std::getenv("IG_MIXED_FLAT")) S->rows_force = std::atoi(v) ? 1 : 0;
     // IG_MIXED_TAIL=0: the last level above the bottom by separate launches
     if (const char* v = std::getenv("IG_MIXED_TAIL")) S->tail_on = std::atoi(v) != 0;
+    // IG_MIXED_TB_LEVELS: how many of the finest levels smooth temporally
+    // blocked, fixed instead of left to the smoother tuner
     if (const char* v = std::getenv("IG_MIXED_TB_LEVELS")) {
       S->tb_levels = std::max(0, std::atoi(v));
       S->tb_auto = false;
