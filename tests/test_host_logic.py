@@ -241,3 +241,37 @@ def test_pa_surf_sidecar_matches_reference(tmp_path):
         assert th.dtype == want.dtype and th.shape == want.shape
         assert np.array_equal(th.view(np.uint32), want.view(np.uint32))
         assert (want < 1).sum() > 5
+
+
+def test_unit_basis_door_routes_by_precision(monkeypatch):
+    """solve_unit_bases_mg (the field cache's fill, build_stl3d.py:835-849):
+    "fp64" converts the bit-exact door's float64 potentials on the host,
+    (phi / v_basis).astype(float32); "mixed" asks the mixed door for unit
+    bases formed on the device; fa_cache.solve_stl3d_bases passes the
+    cache's V_BASIS and tolerance through."""
+    from ion_gym_gb300.physics import multigrid3d as M
+    from ion_gym_gb300.io import fa_cache
+    shape = (3, 4, 5)
+    masks = {1: np.zeros(shape, bool), 2: np.zeros(shape, bool)}
+    masks[1][0, 0, 0] = masks[2][1, 1, 1] = True
+    seen = {}
+
+    def fake_door(masks_, v_basis=1e4, tol=1e-6, verbose=False,
+                  stencil="ghost_linear", only=None, precision=None, **kw):
+        seen["fp64"] = (v_basis, tol, precision)
+        return {i: np.full(shape, 1234.5678901 * i) for i in masks_}
+
+    def fake_mixed(masks_, todo, v_basis, tol, stencil, verbose, unit=False):
+        seen["mixed"] = (v_basis, tol, unit, [i for _, i, _ in todo])
+        return {i: np.full(shape, 0.5, np.float32) for _, i, _ in todo}
+
+    monkeypatch.setattr(M, "solve_bases_mg", fake_door)
+    monkeypatch.setattr(M, "_solve_bases_mixed_door", fake_mixed)
+    got = M.solve_unit_bases_mg(masks, v_basis=1e4, tol=1e-4, precision="fp64")
+    assert seen["fp64"] == (1e4, 1e-4, "fp64")
+    for i in (1, 2):
+        want = (np.full(shape, 1234.5678901 * i) / 1e4).astype(np.float32)
+        assert got[i].dtype == np.float32 and np.array_equal(got[i], want)
+    got = fa_cache.solve_stl3d_bases(masks, precision="mixed")
+    assert seen["mixed"] == (fa_cache.V_BASIS, fa_cache.STL3D_SOLVE_TOL, True, [1, 2])
+    assert sorted(got) == [1, 2] and got[1].dtype == np.float32
