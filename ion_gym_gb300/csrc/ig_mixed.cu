@@ -300,44 +300,83 @@ __device__ __forceinline__ float4 zero_start_e0(const float* gp, const uint8_t* 
                      zero_start_e0(g.w, m.w));
 }
 
+// The right-hand side a cycle reads: g itself, or (FOLD) g + alpha q -- the
+// flexible CG's update of the previous iteration, formed where it is read
+// (k_cg_update's expression, so the same bits).
+template <bool FOLD>
+struct RhsLd {
+  const float* __restrict__ g;
+  const float* __restrict__ q;
+  float al;
+  __device__ __forceinline__ float4 v4(uint32_t o) const {
+    float4 v = ld4(g + o);
+    if (FOLD) {
+      const float4 w = ld4(q + o);
+      v.x = __fmaf_rn(al, w.x, v.x); v.y = __fmaf_rn(al, w.y, v.y);
+      v.z = __fmaf_rn(al, w.z, v.z); v.w = __fmaf_rn(al, w.w, v.w);
+    }
+    return v;
+  }
+  __device__ __forceinline__ float v1(uint32_t o) const {
+    return FOLD ? __fmaf_rn(al, q[o], g[o]) : g[o];
+  }
+};
+__device__ __forceinline__ float4 zero_start_e0(float4 g, uchar4 m) {
+  return make_float4(zero_start_e0(g.x, m.x), zero_start_e0(g.y, m.y), zero_start_e0(g.z, m.z),
+                     zero_start_e0(g.w, m.w));
+}
+
 // Float4 group t (both colours) of the fused first pair, for one problem:
-// e0, g0 and mask its split arrays (colour 1 at + csz).
+// e0, g0 and mask its split arrays (colour 1 at + csz).  FOLD: the
+// right-hand side is g0 + al q0 (the previous CG iteration's update,
+// formed where it is read), and the thread stores it, both colours of its
+// slots, to gout (a different array: neighbouring threads still read g0).
+template <bool FOLD>
 __device__ __forceinline__ void zero_pair_at(float* e0, const float* g0, const uint8_t* mask,
-                                             const SGeo& G, uint32_t t) {
+                                             const SGeo& G, uint32_t t,
+                                             const float* q0 = nullptr, float al = 0.f,
+                                             float* gout = nullptr) {
   const uint32_t ij = fdivu(t, G.dH4);
   const int m0 = 4 * (int)(t - ij * G.dH4.d);
   const int i = (int)fdivu(ij, G.dny);
   const int j = (int)(ij - (uint32_t)i * G.dny.d);
   const uint32_t base = ij * (uint32_t)G.H + m0;
   float* e1 = e0 + G.csz;
-  const float* g1 = g0 + G.csz;
+  const RhsLd<FOLD> r0{g0, q0, al};
+  const RhsLd<FOLD> r1{g0 + G.csz, FOLD ? q0 + G.csz : nullptr, al};
   const uint8_t* k0 = mask;
   const uint8_t* k1 = mask + G.csz;
+  auto m4 = [&](uint32_t o) { return *reinterpret_cast<const uchar4*>(k0 + o); };
   // colour 0 of this thread's slots
-  *reinterpret_cast<float4*>(e0 + base) = zero_start_e0(g0 + base, k0 + base);
+  const float4 g0own = r0.v4(base);
+  const float4 zc = zero_start_e0(g0own, m4(base));
+  *reinterpret_cast<float4*>(e0 + base) = zc;
   // colour 1 of this thread's slots, from the colour-0 values around them
   const uint32_t rxm = ((uint32_t)lo_i(i, G.nx) * G.ny + j) * G.H + m0;
   const uint32_t rxp = ((uint32_t)hi_i(i, G.nx) * G.ny + j) * G.H + m0;
   const uint32_t rym = ((uint32_t)i * G.ny + lo_i(j, G.ny)) * G.H + m0;
   const uint32_t ryp = ((uint32_t)i * G.ny + hi_i(j, G.ny)) * G.H + m0;
-  const float4 xm = zero_start_e0(g0 + rxm, k0 + rxm);
-  const float4 xp = zero_start_e0(g0 + rxp, k0 + rxp);
-  const float4 ym = zero_start_e0(g0 + rym, k0 + rym);
-  const float4 yp = zero_start_e0(g0 + ryp, k0 + ryp);
-  const float4 zc = zero_start_e0(g0 + base, k0 + base);
+  const float4 xm = zero_start_e0(r0.v4(rxm), m4(rxm));
+  const float4 xp = zero_start_e0(r0.v4(rxp), m4(rxp));
+  const float4 ym = zero_start_e0(r0.v4(rym), m4(rym));
+  const float4 yp = zero_start_e0(r0.v4(ryp), m4(ryp));
   const int p = (i + j + 1) & 1;
   float z[5];
   if (p == 0) {
-    z[0] = m0 > 0 ? zero_start_e0(g0[base - 1], k0[base - 1]) : zc.x;
+    z[0] = m0 > 0 ? zero_start_e0(r0.v1(base - 1), k0[base - 1]) : zc.x;
     z[1] = zc.x; z[2] = zc.y; z[3] = zc.z; z[4] = zc.w;
   } else {
     z[0] = zc.x; z[1] = zc.y; z[2] = zc.z; z[3] = zc.w;
-    z[4] = m0 + 4 < G.H ? zero_start_e0(g0[base + 4], k0[base + 4]) : 0.f;
+    z[4] = m0 + 4 < G.H ? zero_start_e0(r0.v1(base + 4), k0[base + 4]) : 0.f;
   }
   const int utop = G.nz - 1 - p - 2 * m0;
   const float sx[4] = {(xm.x + xp.x) + (ym.x + yp.x), (xm.y + xp.y) + (ym.y + yp.y),
                        (xm.z + xp.z) + (ym.z + yp.z), (xm.w + xp.w) + (ym.w + yp.w)};
-  const float4 gg = ld4(g1 + base);
+  const float4 gg = r1.v4(base);
+  if (FOLD) {
+    *reinterpret_cast<float4*>(gout + base) = g0own;
+    *reinterpret_cast<float4*>(gout + G.csz + base) = gg;
+  }
   const uchar4 mk = *reinterpret_cast<const uchar4*>(k1 + base);
   const float gv[4] = {gg.x, gg.y, gg.z, gg.w};
   const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
@@ -355,8 +394,25 @@ k_gs_zero_pair(float* __restrict__ e, const float* __restrict__ g,
                const uint8_t* __restrict__ mask, SGeo G, size_t pstride) {
   const uint32_t t = blockIdx.x * kT + threadIdx.x;
   if (t >= (G.csz >> 2)) return;
-  zero_pair_at(e + blockIdx.y * pstride, g + blockIdx.y * pstride,
-               mask + (size_t)blockIdx.y * G.msplit, G, t);
+  zero_pair_at<false>(e + blockIdx.y * pstride, g + blockIdx.y * pstride,
+                      mask + (size_t)blockIdx.y * G.msplit, G, t);
+}
+
+// k_gs_zero_pair on the finest level of a flexible-CG step's later
+// iterations: the right-hand side g + alpha q (alpha = scal[4b + 1], the
+// previous iteration's step) is formed where it is read and stored to
+// gout, which the rest of the iteration reads as its right-hand side --
+// the g half of k_cg_update folded in.
+__global__ void __launch_bounds__(kT)
+k_gs_zero_pair_fold(float* __restrict__ e, const float* __restrict__ g,
+                    const float* __restrict__ q, const double* __restrict__ scal,
+                    float* __restrict__ gout, const uint8_t* __restrict__ mask, SGeo G,
+                    size_t pstride) {
+  const uint32_t t = blockIdx.x * kT + threadIdx.x;
+  if (t >= (G.csz >> 2)) return;
+  const size_t o = blockIdx.y * pstride;
+  zero_pair_at<true>(e + o, g + o, mask + (size_t)blockIdx.y * G.msplit, G, t, q + o,
+                     (float)scal[4 * blockIdx.y + 1], gout + o);
 }
 
 // ---- temporal blocking: S red-black half-sweeps in one pass -----------------
@@ -1162,7 +1218,7 @@ k_tail_cycle(float* __restrict__ e, const float* __restrict__ g,
   __syncthreads();
   const uint32_t nq = A.csz >> 2;
   // pre-smoothing: the fused first pair from e = 0, then nu1 - 1 pairs
-  for (uint32_t t = tid; t < nq; t += kBottomThreads) zero_pair_at(ae, ag, am, A, t);
+  for (uint32_t t = tid; t < nq; t += kBottomThreads) zero_pair_at<false>(ae, ag, am, A, t);
   __syncthreads();
   for (int q = 1; q < nu1; q++)
     for (int c = 0; c < 2; c++) {
@@ -1749,11 +1805,17 @@ k_cg_matvec(const float* __restrict__ p, const float* __restrict__ g,
 // thread of one colour reads the other colour's p_old while that colour's
 // threads store theirs).  Same expressions as the two kernels, same bits;
 // the same grid (colour in y, problem in z).
+// XM: the x half of the previous iteration's k_cg_update folded in at the
+// thread's own slots, where p_old is read anyway: 0 none, 1 x = alpha p_old
+// (the step's first update: x not read), 2 x += alpha p_old; alpha =
+// scal[4b + 1], still the previous iteration's (k_cg_update's expression).
+template <int XM>
 __global__ void __launch_bounds__(kT, 4)
 k_cg_matvec_dir(const float* __restrict__ z, const float* __restrict__ po,
                 float* __restrict__ pn, const double* __restrict__ scal,
                 const float* __restrict__ g, const uint8_t* __restrict__ mask, SGeo G,
-                float* __restrict__ q, double* __restrict__ part, size_t pstride) {
+                float* __restrict__ q, double* __restrict__ part, size_t pstride,
+                float* __restrict__ x) {
   mask += (size_t)blockIdx.z * G.msplit;
   __shared__ double sh[kT / 32];
   const int c = blockIdx.y;
@@ -1774,6 +1836,14 @@ k_cg_matvec_dir(const float* __restrict__ z, const float* __restrict__ po,
     const uint8_t mv[4] = {mk.x, mk.y, mk.z, mk.w};
     const float4 pv = DirLd{z + own, po + own, b}.v4(base);
     *reinterpret_cast<float4*>(pn + own + base) = pv;
+    if (XM) {
+      const float al = (float)scal[4 * blockIdx.z + 1];
+      const float4 pold = ld4(po + own + base);
+      float4 xv = XM == 2 ? ld4(x + own + base) : make_float4(0.f, 0.f, 0.f, 0.f);
+      xv.x = __fmaf_rn(al, pold.x, xv.x); xv.y = __fmaf_rn(al, pold.y, xv.y);
+      xv.z = __fmaf_rn(al, pold.z, xv.z); xv.w = __fmaf_rn(al, pold.w, xv.w);
+      *reinterpret_cast<float4*>(x + own + base) = xv;
+    }
     const float4 gv = ld4(g + own + base);
     const float pp[4] = {pv.x, pv.y, pv.z, pv.w};
     const float gg[4] = {gv.x, gv.y, gv.z, gv.w};
@@ -1943,8 +2013,9 @@ size_t session_bytes(Dims fine, int bmax, int nmetal = 1) {
   while (true) {
     const size_t csz = (size_t)d.nx * d.ny * (size_t)((((d.nz + 1) / 2) + 3) & ~3L);
     b += (d.n() + 2 * csz) * (size_t)nmetal + 2 * (2 * csz * 4 * (size_t)bmax);
-    // level 0: the flexible CG's correction, two direction buffers and L p
-    if (d.n() == fine.n()) b += 4 * (2 * csz * 4 * (size_t)bmax);
+    // level 0: the flexible CG's correction, two direction buffers, L p and
+    // the second right-hand side buffer
+    if (d.n() == fine.n()) b += 5 * (2 * csz * 4 * (size_t)bmax);
     if (is_bottom(d)) break;
     b += std::max(d.n(), 2 * csz) * 4 * (size_t)bmax;
     d = coarse_of(d);
@@ -1987,6 +2058,9 @@ struct Session {
   // q = L p; dot-product partials and per-problem scalars
   Buf<float> xb, pb, qb;
   Buf<float> pb2;  // the other buffer of the direction (fused dir + matvec)
+  Buf<float> g2;   // the finest level's other right-hand side buffer (fold)
+  bool fold_on = true;     // IG_MIXED_FOLD=0: the separate k_cg_update launches
+  bool fold_next = false;  // the next finest-level zero-start pair folds g += alpha q
   Buf<double> part, scal;
   int method = 1;            // 0: defect correction with `vcycles` cycles,
                              // 1: flexible CG preconditioned by one cycle
@@ -2038,6 +2112,7 @@ struct Session {
     xb.release();
     pb.release();
     pb2.release();
+    g2.release();
     qb.release();
     part.release();
     scal.release();
@@ -2133,7 +2208,10 @@ struct Session {
       const size_t ps = lv[0].pstride * bmax;
       xb.alloc(ps, s);
       pb.alloc(ps, s);
-      if (!flat(lv[0])) pb2.alloc(ps, s);
+      if (!flat(lv[0])) {
+        pb2.alloc(ps, s);
+        g2.alloc(ps, s);
+      }
       qb.alloc(ps, s);
       const size_t nb4 = nblk(lv[0].G.csz / 4), nbn = nblk((uint32_t)lv[0].pstride);
       part.alloc(std::max(4 * nb4, nbn) * bmax, s);
@@ -2340,6 +2418,14 @@ struct Session {
         left -= S2;
       }
       q0 = nu1;
+    } else if (zero && fuse_zero_pair(a) && l == 0 && fold_next) {
+      // the previous CG iteration's g += alpha q, folded in: the updated
+      // right-hand side goes to the other buffer, which becomes the level's
+      k_gs_zero_pair_fold<<<dim3(nblk(a.G.csz / 4), B), kT, 0, s>>>(
+          a.e.p, a.g.p, qb.p, scal.p, g2.p, a.mask.p, a.G, a.pstride);
+      std::swap(a.g.p, g2.p);
+      fold_next = false;
+      q0 = 1;
     } else if (zero && fuse_zero_pair(a)) {
       k_gs_zero_pair<<<dim3(nblk(a.G.csz / 4), B), kT, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G,
                                                               a.pstride);
@@ -2443,13 +2529,26 @@ struct Session {
     const unsigned nbd = std::min(nblk(n / 4), kCgBlocks);
     float* pcur = from_b2 ? pb2.p : pb.p;
     float* pnext = from_b2 ? pb.p : pb2.p;
+    const bool fold = fold_ok();
     for (int it = 0; it < cg_iters; it++) {
+      // with fold, iteration it > 0 takes the previous iteration's
+      // k_cg_update in two halves: g += alpha q in the finest level's
+      // zero-start pair, x += alpha p_old in the direction update
+      fold_next = fold && it > 0;
       vcycle(0, true);  // z = f.e
       k_cg_dot<<<dim3(nbd, B), kT, 0, s>>>(f.e.p, qb.p, part.p, f.pstride, n);
       k_cg_reduce<<<B, kT, 0, s>>>(part.p, (int)nbd, 1, scal.p, 1);
       if (fuse_dir()) {
-        k_cg_matvec_dir<<<dim3(nb4, 2, B), kT, 0, s>>>(f.e.p, pcur, pnext, scal.p, f.g.p,
-                                                      f.mask.p, f.G, qb.p, part.p, f.pstride);
+        const dim3 gm(nb4, 2, B);
+        if (!fold || it == 0)
+          k_cg_matvec_dir<0><<<gm, kT, 0, s>>>(f.e.p, pcur, pnext, scal.p, f.g.p, f.mask.p,
+                                               f.G, qb.p, part.p, f.pstride, nullptr);
+        else if (it == 1)
+          k_cg_matvec_dir<1><<<gm, kT, 0, s>>>(f.e.p, pcur, pnext, scal.p, f.g.p, f.mask.p,
+                                               f.G, qb.p, part.p, f.pstride, xb.p);
+        else
+          k_cg_matvec_dir<2><<<gm, kT, 0, s>>>(f.e.p, pcur, pnext, scal.p, f.g.p, f.mask.p,
+                                               f.G, qb.p, part.p, f.pstride, xb.p);
         std::swap(pcur, pnext);
       } else {
         k_cg_dir<<<gv, kT, 0, s>>>(pcur, f.e.p, scal.p, f.pstride, n);
@@ -2459,7 +2558,9 @@ struct Session {
       k_cg_reduce<<<B, kT, 0, s>>>(part.p, 2 * (int)nb4, 2, scal.p, 0);
       // the last iteration's x += alpha p is folded into the FP64 update
       // below; the first one writes x = alpha p (no zeroing pass)
-      if (it == 0 && cg_iters > 1)
+      if (fold)
+        ;  // taken by the next iteration's zero-start pair and direction update
+      else if (it == 0 && cg_iters > 1)
         k_cg_update<true><<<dim3(nblk(n / 4), B), kT, 0, s>>>(xb.p, f.g.p, pcur, qb.p, scal.p,
                                                              f.pstride, n);
       else if (it + 1 < cg_iters)
@@ -2475,6 +2576,17 @@ struct Session {
   // a step ends with the direction in the other buffer when the fused CG
   // runs an odd number of iterations
   bool step_swaps() const { return method == 1 && fuse_dir() && (cg_iters & 1); }
+
+  // The CG update folded into the next iteration (k_gs_zero_pair_fold,
+  // k_cg_matvec_dir<1|2>): the finest level starts its cycle with the fused
+  // zero-start pair, the direction update is fused, and the iterations are
+  // odd in number, so the right-hand side buffers swap an even number of
+  // times per step and every captured step starts and ends on the same one.
+  bool fold_ok() const {
+    return fold_on && method == 1 && fuse_dir() && g2.p != nullptr && cg_iters > 1 &&
+           (cg_iters & 1) && fuse_zero_pair(lv[0]) && !tb_pre(0, true) && !tail_level(0) &&
+           lv.size() > 1;
+  }
 
   void step() {
     const bool from_b2 = method == 1 && p_in_b2;
@@ -2557,12 +2669,19 @@ struct Session {
     const double n = (double)lv[0].G.n;
     double b = 0.0;
     if (method == 1) {
+      const bool fold = fold_ok();
       for (int it = 0; it < cg_iters; it++) {
         b += cycle_bytes(0, true);
         b += 8.0 * n;                                   // <z, q>
         b += (fuse_dir() ? 21.0 : 33.0) * n;            // direction, L p
-        if (it == 0 && cg_iters > 1) b += 20.0 * n;      // x = a p, g += a q
-        else if (it + 1 < cg_iters) b += 24.0 * n;
+        if (fold) {
+          // q in, the updated g out (zero-start pair); x out / in and out
+          if (it > 0) b += 8.0 * n + (it == 1 ? 4.0 : 8.0) * n;
+        } else if (it == 0 && cg_iters > 1) {
+          b += 20.0 * n;                                // x = a p, g += a q
+        } else if (it + 1 < cg_iters) {
+          b += 24.0 * n;
+        }
       }
       b += (cg_iters > 1 ? 25.0 : 21.0) * n;            // phi += x + a p
     } else {
@@ -2577,7 +2696,8 @@ struct Session {
     // per iteration: dot, two reductions, direction + L p (one launch when
     // fused) and, on all but the last, the CG update; then update64, resid64
     if (method == 1)
-      return 2 + cg_iters * (cycle_launches(0, true) + (fuse_dir() ? 4 : 5)) + (cg_iters - 1);
+      return 2 + cg_iters * (cycle_launches(0, true) + (fuse_dir() ? 4 : 5)) +
+             (fold_ok() ? 0 : cg_iters - 1);
     long n = 2;
     for (int v = 0; v < vcycles; v++) n += cycle_launches(0, v == 0);
     return n;
@@ -2761,6 +2881,8 @@ int open_session(const uint8_t* metal, int nmetal, long nx, long ny, long nz,
     // IG_MIXED_FLAT: 0 = one natural row per warp in the FP64 residual and
     // update, 1 = several rows per warp, unset = by row length
     if (const char* v = std::getenv("IG_MIXED_FLAT")) S->rows_force = std::atoi(v) ? 1 : 0;
+    // IG_MIXED_FOLD=0: the flexible CG's updates by separate launches
+    if (const char* v = std::getenv("IG_MIXED_FOLD")) S->fold_on = std::atoi(v) != 0;
     // IG_MIXED_TAIL=0: the last level above the bottom by separate launches
     if (const char* v = std::getenv("IG_MIXED_TAIL")) S->tail_on = std::atoi(v) != 0;
     // IG_MIXED_TB_LEVELS: how many of the finest levels smooth temporally
@@ -3055,9 +3177,9 @@ int ig_mixed_check_fused(void* handle, int n_problems, long long mismatches[8]) 
       const size_t nparts = 2 * (size_t)B * 2 * nb4;
       Buf<double> part2;
       part2.alloc(nparts, s);
-      k_cg_matvec_dir<<<dim3(nb4, 2, B), kT, 0, s>>>(f.e.p, S->pb.p, S->pb2.p, S->scal.p,
-                                                    f.g.p, f.mask.p, f.G, scrB, part2.p,
-                                                    f.pstride);
+      k_cg_matvec_dir<0><<<dim3(nb4, 2, B), kT, 0, s>>>(f.e.p, S->pb.p, S->pb2.p, S->scal.p,
+                                                       f.g.p, f.mask.p, f.G, scrB, part2.p,
+                                                       f.pstride, nullptr);
       k_cg_dir<<<dim3(nblk((uint32_t)f.pstride), B), kT, 0, s>>>(S->pb.p, f.e.p, S->scal.p,
                                                                  f.pstride, (uint32_t)f.pstride);
       k_cg_matvec<<<dim3(nb4, 2, B), kT, 0, s>>>(S->pb.p, f.g.p, f.mask.p, f.G, scrA,

@@ -178,6 +178,32 @@ def test_tail_cycle_gives_the_separate_launches_bits(shape, n_b):
     assert np.array_equal(got["0"].view(np.uint64), got["1"].view(np.uint64))
 
 
+@pytest.mark.parametrize("shape,n_b", [((41, 37, 45), 4), ((64, 48, 40), 1)])
+def test_folded_cg_updates_give_the_separate_launches_bits(shape, n_b):
+    """The flexible CG's updates folded into the next iteration's zero-start
+    pair (g += alpha q) and direction update (x += alpha p) give the
+    potentials of the separate k_cg_update launches, bit for bit, over
+    several refinement steps."""
+    import os
+    from ion_gym_gb300.physics.mixed import MixedSession
+    masks = _deck(shape, 6)
+    metal = np.zeros(shape, bool)
+    for m in masks.values():
+        metal |= m
+    rings = [masks[i] for i in sorted(masks)][:n_b]
+    got = {}
+    for fold in ("0", "1"):
+        os.environ["IG_MIXED_FOLD"] = fold
+        try:
+            with MixedSession(metal, len(rings)) as s:
+                got[fold] = s.solve_bases(rings, V, ACC)
+                got[fold + "steps"] = s.last_steps
+        finally:
+            del os.environ["IG_MIXED_FOLD"]
+    assert got["1steps"] == got["0steps"] >= 2
+    assert np.array_equal(got["0"].view(np.uint64), got["1"].view(np.uint64))
+
+
 def test_fixed_point_update_conversion_matches_the_hardware():
     """The integer-pipe float -> int64 conversion with which the update adds
     a correction to the fixed-point potential gives the GPU conversion
