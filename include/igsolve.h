@@ -221,6 +221,12 @@ int ig_mixed_solve_values_acc(void *handle, const double *vals, int n_problems,
                               const double *acc, int max_steps, double *phi_out,
                               int *steps_out, double *dmax_out);
 void ig_mixed_close(void *handle);
+/* Changes a session's cycle (no reference counterpart): nu1 / nu2
+ * smoothing pairs before / after the coarse correction and the flexible
+ * CG's iterations per refinement step; the captured graphs are dropped and
+ * recaptured at the next solve, the buffers kept.  The accuracy contract
+ * of the solves is unchanged (their bits follow the cycle). */
+int ig_mixed_set_cycle(void *handle, int nu1, int nu2, int cg_iters);
 /* Gives a session another geometry of its shape (no reference
  * counterpart): the new metal union's masks replace the old ones on every
  * level; the buffers, the tuned smoother shape and the captured graphs stay,

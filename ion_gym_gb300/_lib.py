@@ -101,6 +101,7 @@ SIGNATURES = {
     "ig_mixed_solve_values_acc": (_i, [_p, _p, _i, _p, _i, _p, _pi, _p]),
     "ig_mixed_check_fused": (_i, [_p, _i, ctypes.POINTER(ctypes.c_longlong)]),
     "ig_mixed_solve_bytes": (_i, [_p, ctypes.POINTER(ctypes.c_double)]),
+    "ig_mixed_set_cycle": (_i, [_p, _i, _i, _i]),
     "ig_mixed_tuning": (_i, [_p, _i, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int),
                              ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_double)]),
     "ig_mixed_check_convert": (_i, [_p, ctypes.c_long, ctypes.POINTER(ctypes.c_longlong)]),

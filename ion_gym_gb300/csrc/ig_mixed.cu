@@ -2187,18 +2187,7 @@ struct Session {
     }
     load_metal(metal);
     bottom_omega = (float)omega_of(lv.back().d);
-    // the level just above the bottom cycles in one CTA per problem
-    // (k_tail_cycle) when its arrays fit in shared memory
-    tail_ok = false;
-    if (tail_on && lv.size() >= 2) {
-      const MLevel& ta = lv[lv.size() - 2];
-      const MLevel& tb = lv.back();
-      tail_ok = !flat(ta) && two_or_more(ta) && two_or_more(tb) && smooth_omega == 1.f &&
-                nu1 >= 1 && nu2 >= 1 && tail_smem_bytes(ta.G, tb.G) <= kTailSmemMax;
-      if (tail_ok)
-        MK(cudaFuncSetAttribute(k_tail_cycle, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                (int)kTailSmemMax));
-    }
+    update_tail();
     if (tb_levels > 0) MK(tb_prepare());
     phi.alloc(n * bmax, s);
     fexp.alloc(bmax, s);
@@ -2368,6 +2357,22 @@ struct Session {
   bool fuse_dir() const { return pb2.p != nullptr; }
 
   // The first pre-smoothing pair from e = 0 runs as one fused pass.
+  // The level just above the bottom cycles in one CTA per problem
+  // (k_tail_cycle) when its arrays fit in shared memory; set at build and
+  // when the cycle changes.
+  void update_tail() {
+    tail_ok = false;
+    if (tail_on && lv.size() >= 2) {
+      const MLevel& ta = lv[lv.size() - 2];
+      const MLevel& tb = lv.back();
+      tail_ok = !flat(ta) && two_or_more(ta) && two_or_more(tb) && smooth_omega == 1.f &&
+                nu1 >= 1 && nu2 >= 1 && tail_smem_bytes(ta.G, tb.G) <= kTailSmemMax;
+      if (tail_ok)
+        MK(cudaFuncSetAttribute(k_tail_cycle, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)kTailSmemMax));
+    }
+  }
+
   // level l's cycle from zero runs as k_tail_cycle (l the last level above
   // the bottom, no temporal blocking there)
   bool tail_level(size_t l) const { return tail_ok && l + 2 == lv.size() && !use_tb(l); }
@@ -2951,6 +2956,28 @@ int ig_mixed_rebind(void* handle, const uint8_t* metal, long nx, long ny, long n
   try {
     S->load_metal(metal);             // nmetal masks for a per-problem session
     MK(cudaStreamSynchronize(S->s));  // the caller may reuse its mask buffer
+  } catch (int code) {
+    return code;
+  }
+  return IG_OK;
+}
+
+int ig_mixed_set_cycle(void* handle, int nu1, int nu2, int cg_iters) {
+  set_last_error("");
+  Session* S = static_cast<Session*>(handle);
+  if (!S || nu1 < 0 || nu1 > 16 || nu2 < 1 || nu2 > 16 || cg_iters < 1 || cg_iters > 64) {
+    set_last_error("null session or smoothing pairs outside 0..16 / 1..16, CG iterations "
+                   "outside 1..64");
+    return IG_BAD_ARG;
+  }
+  try {
+    MK(cudaStreamSynchronize(S->s));
+    for (auto& g : S->graphs) cudaGraphExecDestroy(g.second);
+    S->graphs.clear();
+    S->nu1 = nu1;
+    S->nu2 = nu2;
+    S->cg_iters = S->method == 1 ? cg_iters : S->cg_iters;
+    S->update_tail();
   } catch (int code) {
     return code;
   }

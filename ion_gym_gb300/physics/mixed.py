@@ -240,6 +240,15 @@ class MixedSession:
         _lib.check(st, "MixedSession.step_bytes")
         return float(b.value)
 
+    def set_cycle(self, nu1, nu2, cg_iters):
+        """Change the session's cycle (smoothing pairs before and after the
+        coarse correction, CG iterations per refinement step); the next
+        solve recaptures its graphs, the buffers stay."""
+        st = _lib.lib().ig_mixed_set_cycle(self._h, int(nu1), int(nu2), int(cg_iters))
+        _lib.check(st, "MixedSession.set_cycle")
+        self.cycle = {**self.cycle, "nu1": int(nu1), "nu2": int(nu2),
+                      "cg_iters": int(cg_iters)}
+
     def solve_bytes(self):
         """Algorithmic DRAM bytes of every refinement step of the last
         solve."""

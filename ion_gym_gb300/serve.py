@@ -73,6 +73,14 @@ class FieldServer:
     session_factory / bytes_fn: the session class and its footprint
     function (MixedSession and session_bytes; replaceable for tests of the
     admission logic without a GPU).
+    auto_cycle (off by default): a session's second solve tries the other
+    smoothing (three pairs each side of the coarse correction instead of
+    two, or two instead of three), and the session keeps whichever moved
+    fewer algorithmic bytes over its refinement steps (`_tune_cycle`); a
+    rebind to another geometry tries again.  On the board and ring-stack
+    request mix it measured no gain (knee p50 147 against 119 ms,
+    saturation 26.2 against 27.2 requests/s): the trials' graph captures,
+    repeated after every rebind, cost what the boards' cheaper cycle saves.
     results: "host" -- each basis a float64 numpy array (the reference's
     solve_bases_mg return); "device" -- each basis a float64 CUDA tensor
     that stays in HBM for consumers on the GPU (the field build reads bases
@@ -82,10 +90,11 @@ class FieldServer:
 
     def __init__(self, workers=4, hbm_budget=None, device=0,
                  session_factory=MixedSession, bytes_fn=session_bytes,
-                 results="host"):
+                 results="host", auto_cycle=False):
         if results not in ("host", "device"):
             raise ValueError('results must be "host" or "device"')
         self.results = results
+        self.auto_cycle = auto_cycle
         self.device = device
         self._factory = session_factory
         self._bytes_fn = bytes_fn
@@ -206,7 +215,9 @@ class FieldServer:
                     sess = self._factory(metal_of(r.masks, r.shape), r.n_bases)
                 elif rebind:
                     sess.rebind(metal_of(r.masks, r.shape))
+                    sess._cycle_trial = None
                 result, err = self._solve(sess, r), None
+                self._tune_cycle(sess)
             except Exception as e:     # delivered through the future
                 result, err = None, e
             r.end = time.perf_counter()
@@ -231,6 +242,32 @@ class FieldServer:
                 fut.set_exception(err)
             del result, fut
 
+
+    def _tune_cycle(self, sess):
+        """After a solve on a session: the first solve's cycle and the
+        algorithmic bytes of its refinement steps are noted and the other
+        smoothing set; after the second solve the session keeps the cycle
+        whose solve moved fewer bytes (3 % margin, so ties keep the
+        batch-size default).  Bytes rather than time: counted by the
+        session itself, they do not depend on what else the GPU runs.
+        (Planar boards converge in fewer steps with three pairs; the ring
+        stack takes the same steps with two, so it keeps two.)"""
+        if not self.auto_cycle or not hasattr(sess, "set_cycle"):
+            return
+        trial = getattr(sess, "_cycle_trial", None)
+        if trial == "done":
+            return
+        cyc = dict(sess.cycle)
+        cost = sess.solve_bytes()
+        if trial is None:
+            pairs = 3 if (cyc["nu1"], cyc["nu2"]) == (2, 2) else 2
+            sess._cycle_trial = (cyc, cost)
+            sess.set_cycle(pairs, pairs, cyc["cg_iters"])
+        else:
+            first, first_cost = trial
+            if not cost < 0.97 * first_cost:
+                sess.set_cycle(first["nu1"], first["nu2"], first["cg_iters"])
+            sess._cycle_trial = "done"
 
     def _solve(self, sess, r):
         """{index: basis} of a request on its session (host or device

@@ -204,6 +204,26 @@ def test_folded_cg_updates_give_the_separate_launches_bits(shape, n_b):
     assert np.array_equal(got["0"].view(np.uint64), got["1"].view(np.uint64))
 
 
+def test_set_cycle_matches_a_session_opened_with_it():
+    """A session whose cycle is changed after a solve (its graphs dropped
+    and recaptured) gives the bits of a session opened with that cycle."""
+    from ion_gym_gb300.physics.mixed import MixedSession
+    shape = (41, 37, 45)
+    masks = _deck(shape, 8)
+    metal = np.zeros(shape, bool)
+    for m in masks.values():
+        metal |= m
+    rings = [masks[i] for i in sorted(masks)]
+    with MixedSession(metal, len(rings)) as s:
+        s.solve_bases(rings, V, ACC)
+        s.set_cycle(3, 3, 3)
+        got = s.solve_bases(rings, V, ACC)
+        assert s.cycle["nu1"] == 3 and s.cycle["nu2"] == 3
+    with MixedSession(metal, len(rings), nu1=3, nu2=3, cg_iters=3) as s:
+        ref = s.solve_bases(rings, V, ACC)
+    assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
+
+
 def test_fixed_point_update_conversion_matches_the_hardware():
     """The integer-pipe float -> int64 conversion with which the update adds
     a correction to the fixed-point potential gives the GPU conversion

@@ -165,3 +165,40 @@ def test_new_geometry_of_a_resident_shape_rebinds_an_idle_session():
     srv.submit(_deck(4, 2, shape=(7, 5, 4))).result(timeout=10)  # other shape
     assert len(FakeSession.opened) == 3 and len(RebindingSession.rebinds) == 1
     srv.close()
+
+
+def test_sessions_keep_the_cheaper_smoothing():
+    """auto_cycle: a session's second solve tries the other smoothing and
+    the session keeps whichever moved fewer algorithmic bytes (a fake
+    whose bytes depend on the cycle): one geometry cheaper with three
+    pairs keeps three, one cheaper with two returns to two."""
+
+    class CycleSession(FakeSession):
+        def __init__(self, metal, n):
+            super().__init__(metal, n)
+            self.cycle = {"nu1": 2, "nu2": 2, "cg_iters": 3}
+            self.prefer3 = bool(metal[0, 0, 0])
+            self.calls = []
+
+        def set_cycle(self, nu1, nu2, cg_iters):
+            self.calls.append((nu1, nu2, cg_iters))
+            self.cycle = {"nu1": nu1, "nu2": nu2, "cg_iters": cg_iters}
+
+        def solve_bytes(self):
+            three = self.cycle["nu1"] == 3
+            return 80.0 if three == self.prefer3 else 100.0
+
+    srv = FieldServer(workers=1, hbm_budget=10_000, device=None,
+                      session_factory=CycleSession,
+                      bytes_fn=lambda shape, n: 100 * n, auto_cycle=True)
+    a = _deck(1, 2)
+    a[1][0, 0, 0] = True                      # this geometry prefers three
+    b = _deck(2, 2)
+    b[1][0, 0, 0] = b[2][0, 0, 0] = False     # this one prefers two
+    for _ in range(3):
+        srv.submit(a, key="a").result(10)
+        srv.submit(b, key="b").result(10)
+    srv.close()
+    sa, sb = [s for s in CycleSession.opened]
+    assert sa.cycle["nu1"] == 3 and sa.calls == [(3, 3, 3)]
+    assert sb.cycle["nu1"] == 2 and sb.calls == [(3, 3, 3), (2, 2, 3)]
