@@ -1742,6 +1742,48 @@ struct KSum {
   __device__ __forceinline__ double value() const { return (double)s - (double)c; }
 };
 
+// The last half-sweep of the finest level's cycle (k_gs4<NG, false>, the
+// same update) with the flexible CG's <z, q_old> formed in the same pass:
+// once the colour-c groups are updated, z is final, so each thread adds
+// both colours of its slots (the other colour from the half-sweep before)
+// against q, and each block writes one partial (part[b * gridDim.x +
+// blockIdx.x]) -- k_cg_dot's read of z folded into the sweep that writes
+// it.  Summation order differs from k_cg_dot (blocks of the sweep's shape),
+// so the partial sums, not the update, may differ in their last bits.
+template <int NG>
+__global__ void k_gs4_dot(float* __restrict__ e, const float* __restrict__ g,
+                          const uint8_t* __restrict__ mask, SGeo G, int c, float omega,
+                          size_t pstride, const float* __restrict__ q,
+                          double* __restrict__ part) {
+  __shared__ double sh[32];
+  mask += (size_t)blockIdx.y * G.msplit;
+  const uint32_t nq = G.csz >> 2;
+  float* eb = e + blockIdx.y * pstride;
+  float* own = eb + (size_t)c * G.csz;
+  const float* oth = eb + (size_t)(1 - c) * G.csz;
+  const float* gp = g + blockIdx.y * pstride + (size_t)c * G.csz;
+  const uint8_t* mp = mask + (size_t)c * G.csz;
+  const float* qo = q + blockIdx.y * pstride + (size_t)c * G.csz;
+  const float* qt = q + blockIdx.y * pstride + (size_t)(1 - c) * G.csz;
+  const uint32_t t0 = blockIdx.x * blockDim.x * NG + threadIdx.x;
+  KSum acc;
+#pragma unroll
+  for (int u = 0; u < NG; u++) {
+    const uint32_t t = t0 + u * blockDim.x;
+    if (t < nq) {
+      gs4_group<false>(own, oth, gp, mp, G, c, omega, t);
+      const uint32_t ij = fdivu(t, G.dH4);
+      const uint32_t base = ij * (uint32_t)G.H + 4 * (t - ij * G.dH4.d);
+      const float4 za = ld4(own + base), zb = ld4(oth + base);
+      const float4 qa = ld4(qo + base), qb = ld4(qt + base);
+      acc.add(za.x * qa.x); acc.add(za.y * qa.y); acc.add(za.z * qa.z); acc.add(za.w * qa.w);
+      acc.add(zb.x * qb.x); acc.add(zb.y * qb.y); acc.add(zb.z * qb.z); acc.add(zb.w * qb.w);
+    }
+  }
+  const double tot = block_sum_d(acc.value(), sh);
+  if (threadIdx.x == 0) part[(size_t)blockIdx.y * gridDim.x + blockIdx.x] = tot;
+}
+
 // q = L p (both colours; q = 0 on metal) and block partials of <p, q> and
 // <p, g>; blockIdx.y = colour, blockIdx.z = problem.  Grid-stride over
 // float4 groups (kCgBlocks blocks per colour and problem), so each block
@@ -2061,6 +2103,10 @@ struct Session {
   Buf<float> g2;   // the finest level's other right-hand side buffer (fold)
   bool fold_on = true;     // IG_MIXED_FOLD=0: the separate k_cg_update launches
   bool fold_next = false;  // the next finest-level zero-start pair folds g += alpha q
+  bool dot_on = true;      // IG_MIXED_DOT=0: <z, q> by k_cg_dot
+  bool dot_next = false;   // the finest level's last half-sweep forms <z, q>
+  bool dot_done = false;   // ... and did (its partial count in dot_nparts)
+  int dot_nparts = 0;
   Buf<double> part, scal;
   int method = 1;            // 0: defect correction with `vcycles` cycles,
                              // 1: flexible CG preconditioned by one cycle
@@ -2240,6 +2286,32 @@ struct Session {
                                                         a.pstride);
         break;
     }
+  }
+
+  // The finest level's last half-sweep with <z, q> folded in (k_gs4_dot):
+  // its partials go to `part`, their count to dot_nparts.  Returns false
+  // (nothing launched) where the tuned shape has no such form.
+  bool launch_gs_dot(MLevel& a, int c, int nb, float omega) {
+    if (flat(a) || gs_cfg.ng == 8) return false;
+    const uint32_t nq = a.G.csz / 4;
+    const unsigned per = (unsigned)(gs_cfg.threads * gs_cfg.ng);
+    const dim3 grid((nq + per - 1) / per, nb);
+    switch (gs_cfg.ng) {
+      case 4:
+        k_gs4_dot<4><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega,
+                                                      a.pstride, qb.p, part.p);
+        break;
+      case 2:
+        k_gs4_dot<2><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega,
+                                                      a.pstride, qb.p, part.p);
+        break;
+      default:
+        k_gs4_dot<1><<<grid, gs_cfg.threads, 0, s>>>(a.e.p, a.g.p, a.mask.p, a.G, c, omega,
+                                                      a.pstride, qb.p, part.p);
+        break;
+    }
+    dot_nparts = (int)grid.x;
+    return true;
   }
 
   // The smoother's launch shape (groups per thread x block size) and its
@@ -2476,7 +2548,15 @@ struct Session {
       return;
     }
     for (int q = 0; q < nu2; q++)
-      for (int c = 1; c >= 0; c--) launch_gs(a, c, B, smooth_omega);
+      for (int c = 1; c >= 0; c--) {
+        if (l == 0 && dot_next && q + 1 == nu2 && c == 0 &&
+            launch_gs_dot(a, c, B, smooth_omega)) {
+          dot_next = false;
+          dot_done = true;
+          continue;
+        }
+        launch_gs(a, c, B, smooth_omega);
+      }
   }
 
   // the finest level's FP64 residual and potential update, one warp per
@@ -2540,9 +2620,17 @@ struct Session {
       // k_cg_update in two halves: g += alpha q in the finest level's
       // zero-start pair, x += alpha p_old in the direction update
       fold_next = fold && it > 0;
+      dot_next = dot_on;
+      dot_done = false;
       vcycle(0, true);  // z = f.e
-      k_cg_dot<<<dim3(nbd, B), kT, 0, s>>>(f.e.p, qb.p, part.p, f.pstride, n);
-      k_cg_reduce<<<B, kT, 0, s>>>(part.p, (int)nbd, 1, scal.p, 1);
+      dot_next = false;
+      if (dot_done) {
+        // <z, q> was formed by the cycle's last half-sweep
+        k_cg_reduce<<<B, kT, 0, s>>>(part.p, dot_nparts, 1, scal.p, 1);
+      } else {
+        k_cg_dot<<<dim3(nbd, B), kT, 0, s>>>(f.e.p, qb.p, part.p, f.pstride, n);
+        k_cg_reduce<<<B, kT, 0, s>>>(part.p, (int)nbd, 1, scal.p, 1);
+      }
       if (fuse_dir()) {
         const dim3 gm(nb4, 2, B);
         if (!fold || it == 0)
@@ -2587,6 +2675,13 @@ struct Session {
   // zero-start pair, the direction update is fused, and the iterations are
   // odd in number, so the right-hand side buffers swap an even number of
   // times per step and every captured step starts and ends on the same one.
+  // <z, q> formed by the finest level's last half-sweep (k_gs4_dot; the
+  // conditions under which vcycle reaches launch_gs_dot)
+  bool dot_fused() const {
+    return dot_on && method == 1 && lv.size() > 1 && !tail_level(0) && !tb_post(0) &&
+           nu2 >= 1 && !flat(lv[0]) && gs_cfg.ng != 8;
+  }
+
   bool fold_ok() const {
     return fold_on && method == 1 && fuse_dir() && g2.p != nullptr && cg_iters > 1 &&
            (cg_iters & 1) && fuse_zero_pair(lv[0]) && !tb_pre(0, true) && !tail_level(0) &&
@@ -2677,7 +2772,7 @@ struct Session {
       const bool fold = fold_ok();
       for (int it = 0; it < cg_iters; it++) {
         b += cycle_bytes(0, true);
-        b += 8.0 * n;                                   // <z, q>
+        b += (dot_fused() ? 4.0 : 8.0) * n;             // <z, q> (q only when fused)
         b += (fuse_dir() ? 21.0 : 33.0) * n;            // direction, L p
         if (fold) {
           // q in, the updated g out (zero-start pair); x out / in and out
@@ -2701,7 +2796,8 @@ struct Session {
     // per iteration: dot, two reductions, direction + L p (one launch when
     // fused) and, on all but the last, the CG update; then update64, resid64
     if (method == 1)
-      return 2 + cg_iters * (cycle_launches(0, true) + (fuse_dir() ? 4 : 5)) +
+      return 2 + cg_iters * (cycle_launches(0, true) + (fuse_dir() ? 4 : 5) -
+                             (dot_fused() ? 1 : 0)) +
              (fold_ok() ? 0 : cg_iters - 1);
     long n = 2;
     for (int v = 0; v < vcycles; v++) n += cycle_launches(0, v == 0);
@@ -2886,6 +2982,8 @@ int open_session(const uint8_t* metal, int nmetal, long nx, long ny, long nz,
     // IG_MIXED_FLAT: 0 = one natural row per warp in the FP64 residual and
     // update, 1 = several rows per warp, unset = by row length
     if (const char* v = std::getenv("IG_MIXED_FLAT")) S->rows_force = std::atoi(v) ? 1 : 0;
+    // IG_MIXED_DOT=0: the flexible CG's <z, q> by its own kernel
+    if (const char* v = std::getenv("IG_MIXED_DOT")) S->dot_on = std::atoi(v) != 0;
     // IG_MIXED_FOLD=0: the flexible CG's updates by separate launches
     if (const char* v = std::getenv("IG_MIXED_FOLD")) S->fold_on = std::atoi(v) != 0;
     // IG_MIXED_TAIL=0: the last level above the bottom by separate launches

@@ -224,6 +224,31 @@ def test_set_cycle_matches_a_session_opened_with_it():
     assert np.array_equal(got.view(np.uint64), ref.view(np.uint64))
 
 
+@pytest.mark.parametrize("shape,n_b", [((41, 37, 45), 4), ((64, 48, 40), 1)])
+def test_fused_inner_product_keeps_the_accuracy(shape, n_b):
+    """<z, q> formed by the last half-sweep of the finest level (k_gs4_dot)
+    instead of its own kernel sums in another order; the solves take the
+    same refinement steps and agree within the stated accuracy."""
+    import os
+    from ion_gym_gb300.physics.mixed import MixedSession
+    masks = _deck(shape, 9)
+    metal = np.zeros(shape, bool)
+    for m in masks.values():
+        metal |= m
+    rings = [masks[i] for i in sorted(masks)][:n_b]
+    got = {}
+    for dot in ("0", "1"):
+        os.environ["IG_MIXED_DOT"] = dot
+        try:
+            with MixedSession(metal, len(rings)) as s:
+                got[dot] = s.solve_bases(rings, V, ACC)
+                got[dot + "steps"] = s.last_steps
+        finally:
+            del os.environ["IG_MIXED_DOT"]
+    assert got["0steps"] == got["1steps"]
+    assert np.abs(got["0"] - got["1"]).max() <= 2 * ACC * V
+
+
 def test_fixed_point_update_conversion_matches_the_hardware():
     """The integer-pipe float -> int64 conversion with which the update adds
     a correction to the fixed-point potential gives the GPU conversion
